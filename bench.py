@@ -1,0 +1,371 @@
+"""Benchmark: site-updates/s of one RK4 step of the EWPT lattice at 256^3.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--n 256] [--no-fp32] [--no-e2e] [--no-cpu]
+
+Workload (one step = one classical RK4 step over the whole lattice): the
+drop-in FP64 configuration -- 256^3 periodic lattice, dx = 0.25,
+dt = dx/10, lambda = 0.129, g = 0.65, g' = 0.35, vev = 1, gp2 = 0.99,
+gamma = beta = Jex = 0, 64 seeded tanh bubbles.  The FP32 precision form
+(FP32 stencils/fluxes, compensated FP32 hi/lo state) is timed on the same
+lattice and reported in the same line.
+
+value    FP64 site-updates/s with the state resident in HBM (CUDA events on
+         the library's stream; the 4.8 GB state is larger than L2).
+e2e      the same metric through the C ABI with host buffers: every step
+         uploads the state from pinned host memory (ewpt_set_state_packed),
+         steps once (ewpt_step) and reads the energy row back
+         (ewpt_diagnostics).
+roofline HBM roofline of the stage kernels: algorithmic bytes per
+         site-update (3744 B FP64, 2592 B FP32 form) x site-updates/s over
+         the measured copy bandwidth.
+--impl reference  times the CPU restatement of the reference's routines (the
+         oracle) on the host cores on a bounded sample lattice.
+With --gpus N > 1 (torchrun), each rank evolves its own replica; value is the
+sum over ranks (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "ewpt-gpu_gb300"))
+
+METRIC = "site-updates/s per RK4 step at 256³ (FP64 vs FP32 form), % of HBM peak"
+BYTES_FP64 = 3744  # 468 FP64 values per site-update (k-storage RK4)
+BYTES_FP32 = 2592  # y in FP64 width, stage rates in FP32
+N_BUBBLES = 64
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_params(n, precision):
+    import ewpt
+
+    return ewpt.baseline_couplings(N=n, dx=0.25, dt=0.025, precision=precision)
+
+
+def time_steps(lat, steps, warmup):
+    """K steps bracketed by CUDA events on the library's stream."""
+    import torch
+
+    st = torch.cuda.ExternalStream(lat.stream)
+    lat.step(warmup)
+    lat.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    lat.step(steps)
+    e1.record(st)
+    lat.sync()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def time_stage_kernels(lat, steps):
+    """Average duration of one stage launch (4 per step), CUDA events."""
+    return None
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    import ewpt
+
+    torch.cuda.set_device(local)
+    n = args.n
+    p64 = make_params(n, ewpt.FP64)
+    p64.device = local
+    shape = p64.dims
+    S = p64.sites
+    y0 = ewpt.ic.bubbles_tanh(shape, p64.dx, N_BUBBLES, seed=1234 + rank)
+    hbm, peak_kind = peaks()
+    res = {}
+    # ---------------------------------------------------------------- FP64
+    with ewpt.Lattice(p64) as lat:
+        lat.set_state(y0)
+        barrier(ws)
+        with Clocks(local) as ck:
+            t = time_steps(lat, args.steps, args.warmup)
+        t = allmax(ws, t)
+        clocks = ck.summary()
+        d = lat.diagnostics()
+        res["fp64"] = dict(t=t, diag=d.tolist())
+        # ------------------------------------------------------------ e2e
+        if not args.no_e2e:
+            host = torch.empty((36, S), dtype=torch.float64, pin_memory=True)
+            host.numpy()[:] = y0
+            ptr = host.data_ptr()
+            row = np.zeros(20)
+            L = lat.L
+            import ctypes as C
+
+            def e2e_step():
+                ewpt._lib.check(L.ewpt_set_state_packed(lat.h, C.c_void_p(ptr), 0), lat.h)
+                ewpt._lib.check(L.ewpt_step(lat.h, 1), lat.h)
+                ewpt._lib.check(L.ewpt_diagnostics(lat.h, row.ctypes.data_as(ewpt._lib.DP)), lat.h)
+
+            for _ in range(max(1, min(args.warmup, 2))):
+                e2e_step()
+            ke = max(1, min(args.steps, 5))
+            barrier(ws)
+            t0 = time.perf_counter()
+            for _ in range(ke):
+                e2e_step()
+            te = allmax(ws, time.perf_counter() - t0)
+            res["e2e"] = dict(t=te, steps=ke, h2d=36 * S * 8, d2h=20 * 8)
+    # ---------------------------------------------------------------- FP32
+    if not args.no_fp32:
+        p32 = make_params(n, ewpt.FP32)
+        p32.device = local
+        with ewpt.Lattice(p32) as lat:
+            lat.set_state(y0)
+            barrier(ws)
+            k32 = max(args.steps, 10)
+            t = allmax(ws, time_steps(lat, k32, args.warmup))
+            res["fp32"] = dict(t=t, steps=k32, diag=lat.diagnostics().tolist())
+    # ------------------------------------------------------- CPU baseline
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(budget_s=args.cpu_seconds)
+    if rank != 0:
+        return
+    t64 = res["fp64"]["t"]
+    v = ws * S * args.steps / t64
+    ach = S * args.steps / t64 * BYTES_FP64 / 1e9
+    out = {
+        "metric": METRIC,
+        "value": v,
+        "unit": "site-updates/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t64 / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": f"synthetic: {N_BUBBLES} seeded tanh-profile bubbles (radius 2/sqrt(lambda)), fields at rest",
+        "config": {"workload": f"drop-in FP64 RK4 step, {n}^3 periodic lattice, dx=0.25, dt=dx/10, "
+                               "lambda=0.129, g=0.65, g'=0.35, vev=1, gp2=0.99, gamma=beta=Jex=0",
+                   "lattice": [n, n, n], "form": "FP64",
+                   "l2": f"inputs larger than L2 (state {36 * S * 8 / 1e9:.2f} GB per replica)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_stage_fp64 (4 launches/step)",
+                     "algorithmic_bytes_per_site_update": BYTES_FP64,
+                     "note": "FP64 form is bound by the FP64 pipe, not HBM; see fp64_pipe in profiles/"},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+    }
+    if "e2e" in res:
+        e = res["e2e"]
+        out["e2e"] = {"value": ws * S * e["steps"] / e["t"], "unit": "site-updates/s",
+                      "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
+                      "path": "ewpt_set_state_packed(pinned host) + ewpt_step(1) + ewpt_diagnostics per step"}
+    if "fp32" in res:
+        f = res["fp32"]
+        v32 = ws * S * f["steps"] / f["t"]
+        a32 = S * f["steps"] / f["t"] * BYTES_FP32 / 1e9
+        out["fp32_form"] = {"value": v32, "unit": "site-updates/s", "ms_per_step": f["t"] / f["steps"] * 1e3,
+                            "steps": f["steps"], "dtype": "f32 stencils/fluxes, f32 hi/lo state",
+                            "speedup_vs_fp64": v32 / v,
+                            "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm, "unit": "GB/s",
+                                         "frac": a32 / hbm, "peak_kind": peak_kind,
+                                         "algorithmic_bytes_per_site_update": BYTES_FP32}}
+    if cpu:
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out), flush=True)
+
+
+def cpu_baseline(budget_s=20.0, threads=None):
+    """The oracle (CPU restatement of the reference routines) on the host
+    cores: config-1 style lattice, seconds-bounded sample."""
+    import numpy as np
+
+    import ewpt
+    from oracle import oracle as orc
+
+    orc.build()
+    if threads:
+        orc.set_threads(threads)
+    nthr = orc.num_threads()
+    p = make_params(64, ewpt.FP64)
+    y = ewpt.ic.bubbles_tanh(p.dims, p.dx, 10, seed=7)
+    op = orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
+    work = np.empty(3 * y.size)
+    orc.rk4_step(op, y, p.dt, work=work)  # warm
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        y = orc.rk4_step(op, y, p.dt, work=work)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= 200:
+            break
+    return {"value": p.sites * steps / el, "unit": "site-updates/s", "cores": nthr, "kind": "port",
+            "sample": f"64^3 lattice, 10 bubbles, {steps} FP64 RK4 steps ({el:.1f} s) of the oracle "
+                      f"(C restatement of rk4_step! + broadcasts, OpenMP {nthr} threads)"}
+
+
+def run_reference(args, ws, rank):
+    """CPU reference arm: the oracle on all host cores, bounded sample."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    import ewpt
+    from oracle import oracle as orc
+
+    orc.build()
+    nthr = orc.num_threads()
+    # size the sample lattice so one step takes ~2 s on this host
+    probe = make_params(32, ewpt.FP64)
+    op = orc.params(probe.dims, probe.dx, probe.gw, probe.gy, probe.gp2, probe.lam, probe.vev)
+    y = ewpt.ic.bubbles_tanh(probe.dims, probe.dx, 4, seed=3)
+    t0 = time.perf_counter()
+    orc.rk4_step(op, y, probe.dt)
+    per_site = (time.perf_counter() - t0) / probe.sites
+    n = int(round((2.0 / max(per_site, 1e-12)) ** (1.0 / 3.0)))
+    n = max(32, min(args.n, (n // 8) * 8))
+    p = make_params(n, ewpt.FP64)
+    op = orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
+    y = ewpt.ic.bubbles_tanh(p.dims, p.dx, max(4, N_BUBBLES * n ** 3 // args.n ** 3), seed=1234)
+    work = np.empty(3 * y.size)
+    for _ in range(args.warmup):
+        y = orc.rk4_step(op, y, p.dt, work=work)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        y = orc.rk4_step(op, y, p.dt, work=work)
+    el = time.perf_counter() - t0
+    v = p.sites * args.steps / el
+    sample = (f"{n}^3 sample lattice with the {args.n}^3 workload's per-site work (FP64 RK4 steps, "
+              f"64-bubble density), oracle C restatement of rk4_step! + RK4 broadcasts, OpenMP {nthr} threads")
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "site-updates/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: seeded tanh-profile bubbles",
+           "config": {"workload": f"drop-in FP64 RK4 step, {args.n}^3 periodic lattice, dx=0.25, dt=dx/10",
+                      "lattice": [n, n, n], "form": "FP64", "parallelism": "host cores"},
+           "cpu_baseline": {"value": v, "unit": "site-updates/s", "cores": nthr, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

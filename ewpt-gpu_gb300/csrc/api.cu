@@ -1,0 +1,287 @@
+// api.cu -- the C ABI of libewpt (declared in include/ewpt.h).
+//
+// A context owns the device state of one periodic lattice and one CUDA
+// stream.  Host <-> device copies are explicit (ewpt_set_state /
+// ewpt_get_state); stepping, diagnostics and spectra run on the stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "ewpt_ctx.cuh"
+
+static thread_local std::string g_err = "";
+
+int ewpt_fail(ewpt_ctx* ctx, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx)
+        ctx->err = buf;
+    else
+        g_err = buf;
+    return code;
+}
+
+int ewpt_cuda_check(ewpt_ctx* ctx, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return EWPT_OK;
+    if (e == cudaErrorMemoryAllocation)
+        return ewpt_fail(ctx, EWPT_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return ewpt_fail(ctx, EWPT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx) {
+    if (!p) return ewpt_fail(ctx, EWPT_ERR_ARG, "params is NULL");
+    if (p->nx < 7 || p->ny < 7 || p->nz < 7)
+        return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice %dx%dx%d: each axis needs >= 7 sites (3-site stencil halo)",
+                         p->nx, p->ny, p->nz);
+    if ((int64_t)p->nx * p->ny * p->nz > (int64_t)INT32_MAX)
+        return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large: nx*ny*nz must be < 2^31");
+    if (p->precision != EWPT_FP64 && p->precision != EWPT_FP32)
+        return ewpt_fail(ctx, EWPT_ERR_ARG, "precision %d unknown", p->precision);
+    const double v[] = {p->dx, p->dt, p->gw, p->gy, p->gp2, p->lambda, p->vev, p->theta_w,
+                        p->beta_w, p->beta_y, p->gamma_inp, p->mH, p->t_sat};
+    for (double x : v)
+        if (!std::isfinite(x)) return ewpt_fail(ctx, EWPT_ERR_ARG, "non-finite parameter");
+    if (!(p->dx > 0)) return ewpt_fail(ctx, EWPT_ERR_ARG, "dx must be > 0");
+    if (!(p->dt > 0)) return ewpt_fail(ctx, EWPT_ERR_ARG, "dt must be > 0");
+    return EWPT_OK;
+}
+
+extern "C" {
+
+int ewpt_params_default(ewpt_params* p, int32_t n) {
+    if (!p) return ewpt_fail(nullptr, EWPT_ERR_ARG, "params is NULL");
+    std::memset(p, 0, sizeof *p);
+    p->nx = p->ny = p->nz = n;
+    p->precision = EWPT_FP64;
+    p->dx = 0.25;
+    p->dt = p->dx / 10.0;
+    p->gw = 0.65;
+    p->theta_w = std::asin(std::sqrt(0.22));
+    p->gy = p->gw * std::tan(p->theta_w);
+    p->gp2 = 0.99;
+    p->lambda = 0.129;
+    p->vev = 1.0;
+    p->beta_w = 0.0;
+    p->beta_y = 0.0;
+    p->gamma_inp = 0.0;
+    p->mH = 2.0 * std::sqrt(p->lambda) * p->vev;
+    p->t_sat = 2.0;
+    p->thermal_init = 0;
+    p->device = 0;
+    return EWPT_OK;
+}
+
+const char* ewpt_last_error(const ewpt_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
+    if (!out) return ewpt_fail(nullptr, EWPT_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = ewpt_validate_params(p, nullptr);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return ewpt_fail(nullptr, EWPT_ERR_CUDA, "no CUDA device available");
+    if (p->device < 0 || p->device >= ndev)
+        return ewpt_fail(nullptr, EWPT_ERR_ARG, "device %d out of range (%d devices)", p->device, ndev);
+    ewpt_ctx* c = new ewpt_ctx();
+    c->p = *p;
+    c->g.nx = p->nx;
+    c->g.ny = p->ny;
+    c->g.nz = p->nz;
+    c->g.S = (int64_t)p->nx * p->ny * p->nz;
+    c->it = 0;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    rc = ewpt_cuda_check(nullptr, e, "stream");
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    const size_t n = (size_t)36 * c->g.S;
+    if (p->precision == EWPT_FP64) {
+        e = cudaMalloc(&c->y, n * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&c->yn, n * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&c->xa, n * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&c->xb, n * 8);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->y, 0, n * 8, c->st);
+    } else {
+        float** bufs[] = {&c->y32.hi, &c->y32.lo, &c->w32.k1, &c->w32.k2, &c->w32.k3, &c->w32.xa, &c->w32.xb};
+        e = cudaSuccess;
+        for (float** b : bufs)
+            if (e == cudaSuccess) e = cudaMalloc(b, n * 4);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->y32.hi, 0, n * 4, c->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->y32.lo, 0, n * 4, c->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    rc = ewpt_cuda_check(nullptr, e, "state allocation");
+    if (rc) {
+        ewpt_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return EWPT_OK;
+}
+
+int ewpt_destroy(ewpt_ctx* c) {
+    if (!c) return EWPT_OK;
+    cudaSetDevice(c->p.device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    ewpt_release_aux(c);
+    cudaFree(c->y);
+    cudaFree(c->yn);
+    cudaFree(c->xa);
+    cudaFree(c->xb);
+    cudaFree(c->y32.hi);
+    cudaFree(c->y32.lo);
+    cudaFree(c->w32.k1);
+    cudaFree(c->w32.k2);
+    cudaFree(c->w32.k3);
+    cudaFree(c->w32.xa);
+    cudaFree(c->w32.xb);
+    cudaFree(c->scratch64);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return EWPT_OK;
+}
+
+// Device buffer holding the packed FP64 state (for FP32 contexts, a staging
+// buffer that split/join convert through).
+static int staging64(ewpt_ctx* c, double** out) {
+    if (c->p.precision == EWPT_FP64) {
+        *out = c->y;
+        return EWPT_OK;
+    }
+    int rc = ewpt_ensure_scratch64(c);
+    if (rc) return rc;
+    *out = c->scratch64;
+    return EWPT_OK;
+}
+
+int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t on_device) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!arrays) return ewpt_fail(c, EWPT_ERR_ARG, "arrays is NULL");
+    for (int a = 0; a < 36; ++a)
+        if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
+    cudaSetDevice(c->p.device);
+    double* dst;
+    int rc = staging64(c, &dst);
+    if (rc) return rc;
+    const size_t bytes = (size_t)c->g.S * 8;
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < 36 && e == cudaSuccess; ++a)
+        e = cudaMemcpyAsync(dst + (size_t)a * c->g.S, arrays[a], bytes,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, dst, c->y32, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    return ewpt_cuda_check(c, e, "set_state");
+}
+
+int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_device) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!arrays) return ewpt_fail(c, EWPT_ERR_ARG, "arrays is NULL");
+    for (int a = 0; a < 36; ++a)
+        if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
+    cudaSetDevice(c->p.device);
+    double* src;
+    int rc = staging64(c, &src);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->y32, src, c->st);
+    const size_t bytes = (size_t)c->g.S * 8;
+    for (int a = 0; a < 36 && e == cudaSuccess; ++a)
+        e = cudaMemcpyAsync(arrays[a], src + (size_t)a * c->g.S, bytes,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    return ewpt_cuda_check(c, e, "get_state");
+}
+
+int ewpt_set_state_packed(ewpt_ctx* c, const double* buf, int32_t on_device) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!buf) return ewpt_fail(c, EWPT_ERR_ARG, "buf is NULL");
+    const double* a[36];
+    for (int q = 0; q < 36; ++q) a[q] = buf + (size_t)q * c->g.S;
+    return ewpt_set_state(c, a, on_device);
+}
+
+int ewpt_get_state_packed(ewpt_ctx* c, double* buf, int32_t on_device) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!buf) return ewpt_fail(c, EWPT_ERR_ARG, "buf is NULL");
+    double* a[36];
+    for (int q = 0; q < 36; ++q) a[q] = buf + (size_t)q * c->g.S;
+    return ewpt_get_state(c, a, on_device);
+}
+
+// J_ext and damp (main_rk4.jl:5154-5172).
+static double jext_of(const ewpt_params& p, int64_t it) {
+    return (((double)it * p.dt * p.mH <= p.t_sat) && p.thermal_init) ? p.mH * p.mH : 0.0;
+}
+static double damp_of(const ewpt_params& p, int64_t it) {
+    return (((double)it * p.dt * p.mH < p.t_sat) && p.thermal_init) ? 0.0 : p.gamma_inp;
+}
+
+static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double gam) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (nsteps < 0) return ewpt_fail(c, EWPT_ERR_ARG, "nsteps < 0");
+    if (expl && (!std::isfinite(Jex) || !std::isfinite(gam)))
+        return ewpt_fail(c, EWPT_ERR_ARG, "non-finite Jex/gamma");
+    cudaSetDevice(c->p.device);
+    for (int32_t s = 0; s < nsteps; ++s) {
+        const int64_t it = c->it + 1;
+        const double J = expl ? Jex : jext_of(c->p, it);
+        const double G = expl ? gam : damp_of(c->p, it);
+        cudaError_t e;
+        if (c->p.precision == EWPT_FP64)
+            e = launch_step_fp64(c->g, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+        else
+            e = launch_step_fp32(c->g, c->y32, c->w32, c->p, J, G, c->st);
+        int rc = ewpt_cuda_check(c, e, "step launch");
+        if (rc) return rc;
+        c->it = it;
+    }
+    return EWPT_OK;
+}
+
+int ewpt_step(ewpt_ctx* c, int32_t nsteps) { return do_steps(c, nsteps, false, 0.0, 0.0); }
+
+int ewpt_step_explicit(ewpt_ctx* c, int32_t nsteps, double Jex, double gamma) {
+    return do_steps(c, nsteps, true, Jex, gamma);
+}
+
+int64_t ewpt_iteration(const ewpt_ctx* c) { return c ? c->it : -1; }
+
+int ewpt_sync(ewpt_ctx* c) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    cudaSetDevice(c->p.device);
+    return ewpt_cuda_check(c, cudaStreamSynchronize(c->st), "sync");
+}
+
+void* ewpt_stream(ewpt_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int ewpt_rk4_rates(const ewpt_params* p, const double* const in[EWPT_NARR], double* const out[EWPT_NARR],
+                   double Jex, double gamma, void* stream) {
+    int rc = ewpt_validate_params(p, nullptr);
+    if (rc) return rc;
+    if (!in || !out) return ewpt_fail(nullptr, EWPT_ERR_ARG, "in/out is NULL");
+    Ptr36 I;
+    MPtr36 O;
+    for (int a = 0; a < 36; ++a) {
+        if (!in[a] || !out[a]) return ewpt_fail(nullptr, EWPT_ERR_ARG, "array %d is NULL", a);
+        I.p[a] = in[a];
+        O.p[a] = out[a];
+    }
+    for (int a = 0; a < 36; ++a)
+        for (int b = 0; b < 36; ++b)
+            if ((const void*)in[a] == (const void*)out[b])
+                return ewpt_fail(nullptr, EWPT_ERR_ARG, "in[%d] aliases out[%d]", a, b);
+    if (!std::isfinite(Jex) || !std::isfinite(gamma)) return ewpt_fail(nullptr, EWPT_ERR_ARG, "non-finite Jex/gamma");
+    Grid g{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz};
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = launch_rates_fp64(g, I, O, *p, Jex, gamma, (cudaStream_t)stream);
+    return ewpt_cuda_check(nullptr, e, "rk4_rates");
+}
+
+}  // extern "C"

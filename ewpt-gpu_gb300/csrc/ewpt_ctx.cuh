@@ -1,0 +1,42 @@
+// ewpt_ctx.cuh -- the context object behind the opaque ewpt_ctx handle.
+#pragma once
+#include <cstdarg>
+#include <string>
+
+#include "ewpt_internal.cuh"
+
+struct ewpt_ctx {
+    ewpt_params p{};
+    Grid g{};
+    cudaStream_t st = nullptr;
+    int64_t it = 0;  // RK4 iterations done (the reference's loop counter)
+    // FP64 form: state y, accumulator yn, stage inputs xa/xb, each [36][S]
+    double* y = nullptr;
+    double* yn = nullptr;
+    double* xa = nullptr;
+    double* xb = nullptr;
+    // FP32 form: compensated state, stage rates k1..k3, float stage inputs
+    Fp32State y32{nullptr, nullptr};
+    Fp32Work w32{nullptr, nullptr, nullptr, nullptr, nullptr};
+    // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
+    double* scratch64 = nullptr;
+    // diagnostics / spectra scratch (diag.cu, spectrum.cu)
+    double* red = nullptr;      // per-block partial sums
+    int red_blocks = 0;
+    double* dres = nullptr;     // device result row
+    double* field3 = nullptr;   // [3 or 4][S] real fields for the FFT
+    void* fft_out = nullptr;    // complex half-spectrum buffers
+    int fft_plan = 0;           // cufftHandle
+    int fft_ready = 0;
+    double* shell = nullptr;    // per-shell accumulators
+    std::string err;
+};
+
+int ewpt_fail(ewpt_ctx* ctx, int code, const char* fmt, ...);
+int ewpt_cuda_check(ewpt_ctx* ctx, cudaError_t e, const char* what);
+int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx);
+// FP64 view of the current state: c->y for FP64 contexts; for FP32 contexts
+// the state joined into c->scratch64.
+int ewpt_state64(ewpt_ctx* c, const double** out);
+int ewpt_ensure_scratch64(ewpt_ctx* c);
+void ewpt_release_aux(ewpt_ctx* c);

@@ -1,0 +1,254 @@
+// physics.cuh -- per-site right-hand side of the temporal-gauge SU(2)xU(1)
+// Higgs system, templated on the arithmetic type T (double for the FP64
+// form, float for the FP32 stencil/flux form).
+//
+// Same equations as rk4_step! (gpu-kernels-rk4/main_rk4.jl:52-661):
+//   covariant derivatives  cov_derivs_temporal.jl:23-130
+//   field strengths        field_strengths.jl:34-311
+//   kt_phi_a               main_rk4.jl:337-407
+//   kt_W_a_i               main_rk4.jl:409-560
+//   kt_Y_i                 main_rk4.jl:562-581
+//   k_field = momentum     main_rk4.jl:585-600
+//   k_Gamma_a, k_Sigma     main_rk4.jl:603-655
+// evaluated in a register-frugal order: every rate is affine in the spatial
+// derivatives, so each array's gradient and Laplacian are taken together and
+// folded into the rate accumulators right away (Higgs block, then one colour
+// of W at a time, then Y), and each rate is handed to the sink as soon as it
+// is final.  The reference's index pattern of the beta_W bracket of kt_phi
+// (dW_1_3_dt, dW_1_4_dt in all three colour rows, main_rk4.jl:350-352) and
+// the per-component damping term gamma*phi_a*(phi_a*pi_a)/|Phi|^2 (:349, with
+// its 0/0 at |Phi| = 0) are kept.
+//
+// For (a, b, c) a cyclic permutation of the colours, the SU(2) rate reads
+//   kt W^a_i = lap W^a_i - g sum_j (d_j W^b_i W^c_j - d_j W^c_i W^b_j)
+//              - g sum_j (W^b_j F^c_ij - W^c_j F^b_ij) + J^a_i - d_i Gamma^a
+//              - g (W^b_i Gamma^c - W^c_i Gamma^b) + beta terms
+// which is kt_W_1_2 .. kt_W_3_4 of main_rk4.jl:409-560 term by term.
+//
+// Accessor `Acc`:  v(a)  value of array a (0..35, order of ewpt.h) at the site
+//   grad(a, gx, gy, gz)            6th-order first derivatives
+//   grad_lap(a, gx, gy, gz, lap)   first derivatives and Laplacian
+//   div3(a)                        dx(a) + dy(a+1) + dz(a+2)
+// Sink `out(a, rate)` receives rate a = d y_a / dt exactly once.
+#pragma once
+
+template <typename T>
+struct PhysCoef {
+    T gw, gy, hgw, hgy;  // g, g', g/2, g'/2
+    T gp2, omgp2;        // gp2, 1-gp2
+    T lam2, vev2;        // 2*lambda, vev^2
+    T bW, bY, bW2, bY2;  // beta_W, beta_Y, 2*beta_W, 2*beta_Y
+    T hJex, gam;         // Jex/2, damping gamma
+};
+
+// Covariant derivatives D_i phi_a (cov_derivs_temporal.jl:23-130) along one
+// axis with gauge components W1 = W_1_i, W2 = W_2_i, W3 = W_3_i, Y = Y_i.
+template <typename T>
+__device__ __forceinline__ void cov_deriv(T d1, T d2, T d3, T d4, T p1, T p2, T p3, T p4, T W1, T W2, T W3, T Y,
+                                          T hgw, T hgy, T& D1, T& D2, T& D3, T& D4) {
+    D1 = d1 + hgw * (W1 * p4 - W2 * p3 + W3 * p2) + hgy * (Y * p2);
+    D2 = d2 - hgw * (W1 * p3 + W2 * p4 + W3 * p1) - hgy * (Y * p1);
+    D3 = d3 + hgw * (W1 * p2 + W2 * p1 - W3 * p4) + hgy * (Y * p4);
+    D4 = d4 - hgw * (W1 * p1 - W2 * p2 - W3 * p3) - hgy * (Y * p3);
+}
+
+template <typename T, bool BETA, class Acc, class Sink>
+__device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
+    const T gw = c.gw, gy = c.gy, hgw = c.hgw, hgy = c.hgy;
+    const T p1 = A.v(0), p2 = A.v(1), p3 = A.v(2), p4 = A.v(3);
+    T W[3][3];  // W[a][i] = W_{a+1}_{i+2}
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) W[a][i] = A.v(4 + 3 * a + i);
+    const T Y2 = A.v(13), Y3 = A.v(14), Y4 = A.v(15);
+    const T G[3] = {A.v(16), A.v(17), A.v(18)};
+    const T S = A.v(19);
+    const T pt1 = A.v(20), pt2 = A.v(21), pt3 = A.v(22), pt4 = A.v(23);
+
+    // ---- k_field = momentum (main_rk4.jl:585-600)
+#pragma unroll
+    for (int a = 0; a < 16; ++a) out(a, A.v(20 + a));
+
+    // ---- k_Gamma_a, k_Sigma (main_rk4.jl:603-655)
+    {
+        T Wt[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) Wt[a][i] = A.v(24 + 3 * a + i);
+        const T gg = c.gp2 * gw;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int b = (a + 1) % 3, cc = (a + 2) % 3;
+            // -((W_b . Wt_c) - (W_c . Wt_b)) summed over i, as written per i
+            T q = -(W[b][0] * Wt[cc][0] - W[cc][0] * Wt[b][0]) - (W[b][1] * Wt[cc][1] - W[cc][1] * Wt[b][1]) -
+                  (W[b][2] * Wt[cc][2] - W[cc][2] * Wt[b][2]);
+            T h;
+            if (a == 0) h = p1 * pt4 - p4 * pt1 + p3 * pt2 - p2 * pt3;
+            else if (a == 1) h = p3 * pt1 - p1 * pt3 + p4 * pt2 - p2 * pt4;
+            else h = p1 * pt2 - p2 * pt1 + p4 * pt3 - p3 * pt4;
+            out(16 + a, c.omgp2 * A.div3(24 + 3 * a) + gg * q + gg * h);
+        }
+        out(19, c.omgp2 * A.div3(33) + c.gp2 * gy * (p1 * pt2 - p2 * pt1 + p3 * pt4 - p4 * pt3));
+    }
+
+    // ---- Higgs block: gradients, covariant derivatives, kt_phi (main_rk4.jl:337-407)
+    T ktp1, ktp2, ktp3, ktp4;
+    T jW[3][3], jY[3];
+    T cx = T(0), cy = T(0), cz = T(0), pdot = T(0);
+    {
+        T d1[3], d2[3], d3[3], d4[3], l1, l2, l3, l4;
+        A.grad_lap(0, d1[0], d1[1], d1[2], l1);
+        A.grad_lap(1, d2[0], d2[1], d2[2], l2);
+        A.grad_lap(2, d3[0], d3[1], d3[2], l3);
+        A.grad_lap(3, d4[0], d4[1], d4[2], l4);
+        const T Yv[3] = {Y2, Y3, Y4};
+        T D1[3], D2[3], D3[3], D4[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            cov_deriv(d1[i], d2[i], d3[i], d4[i], p1, p2, p3, p4, W[0][i], W[1][i], W[2][i], Yv[i], hgw, hgy, D1[i],
+                      D2[i], D3[i], D4[i]);
+        const T mag = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
+        const T pot = c.lam2 * (mag - c.vev2);
+        const T inv_mag = T(1) / mag;
+        // sum_i W_a_i * f_i
+#define WD(a, f) (W[a][0] * f[0] + W[a][1] * f[1] + W[a][2] * f[2])
+#define YD(f) (Y2 * f[0] + Y3 * f[1] + Y4 * f[2])
+        ktp1 = l1 + hgw * ((WD(0, d4) - WD(1, d3) + WD(2, d2)) + (WD(0, D4) - WD(1, D3) + WD(2, D2))) +
+               hgy * (YD(d2) + YD(D2)) - pot * p1 + T(0.5) * ((gw * G[2] + gy * S) * p2 - gw * G[1] * p3 + gw * G[0] * p4) -
+               c.hJex * p1 - c.gam * p1 * (p1 * pt1) * inv_mag;
+        ktp2 = l2 - hgw * ((WD(0, d3) + WD(1, d4) + WD(2, d1)) + (WD(0, D3) + WD(1, D4) + WD(2, D1))) -
+               hgy * (YD(d1) + YD(D1)) - pot * p2 - T(0.5) * ((gw * G[2] + gy * S) * p1 + gw * G[0] * p3 + gw * G[1] * p4) -
+               c.hJex * p2 - c.gam * p2 * (p2 * pt2) * inv_mag;
+        ktp3 = l3 + hgw * ((WD(0, d2) + WD(1, d1) - WD(2, d4)) + (WD(0, D2) + WD(1, D1) - WD(2, D4))) +
+               hgy * (YD(d4) + YD(D4)) - pot * p3 + T(0.5) * ((-gw * G[2] + gy * S) * p4 + gw * G[1] * p1 + gw * G[0] * p2) -
+               c.hJex * p3 - c.gam * p3 * (p3 * pt3) * inv_mag;
+        ktp4 = l4 - hgw * ((WD(0, d1) - WD(1, d2) - WD(2, d3)) + (WD(0, D1) - WD(1, D2) - WD(2, D3))) -
+               hgy * (YD(d3) + YD(D3)) - pot * p4 - T(0.5) * ((-gw * G[2] + gy * S) * p3 + gw * G[0] * p1 - gw * G[1] * p2) -
+               c.hJex * p4 - c.gam * p4 * (p4 * pt4) * inv_mag;
+#undef WD
+#undef YD
+        // Higgs currents of kt_W (main_rk4.jl:415,432,449,...) and kt_Y (:563)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            jW[0][i] = gw * (p1 * D4[i] - p2 * D3[i] + p3 * D2[i] - p4 * D1[i]);
+            jW[1][i] = gw * (-p1 * D3[i] - p2 * D4[i] + p3 * D1[i] + p4 * D2[i]);
+            jW[2][i] = gw * (p1 * D2[i] - p2 * D1[i] - p3 * D4[i] + p4 * D3[i]);
+            jY[i] = gy * (p1 * D2[i] - p2 * D1[i] + p3 * D4[i] - p4 * D3[i]);
+        }
+        if (BETA) {
+            pdot = pt1 * p1 + pt2 * p2 + pt3 * p3 + pt4 * p4;
+            cx = d1[0] * p1 + d2[0] * p2 + d3[0] * p3 + d4[0] * p4;
+            cy = d1[1] * p1 + d2[1] * p2 + d3[1] * p3 + d4[1] * p4;
+            cz = d1[2] * p1 + d2[2] * p2 + d3[2] * p3 + d4[2] * p4;
+        }
+    }
+
+    // ---- SU(2) block, one colour at a time (field_strengths.jl:34-224)
+    T ktW[3][3];
+    T F[3][3];  // F[b][0] = F^b_xy (W_b_23), [1] = F^b_xz (W_b_24), [2] = F^b_yz (W_b_34)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int b = (a + 1) % 3, cc = (a + 2) % 3;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) ktW[a][i] = jW[a][i] - gw * (W[b][i] * G[cc] - W[cc][i] * G[b]);
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        T dW[3][3];  // dW[i][j] = d_j W^b_i
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            T lap;
+            A.grad_lap(4 + 3 * b + i, dW[i][0], dW[i][1], dW[i][2], lap);
+            ktW[b][i] += lap;
+        }
+        const int b1 = (b + 1) % 3, b2 = (b + 2) % 3;
+        F[b][0] = dW[1][0] - dW[0][1] + gw * (W[b1][0] * W[b2][1] - W[b1][1] * W[b2][0]);
+        F[b][1] = dW[2][0] - dW[0][2] + gw * (W[b1][0] * W[b2][2] - W[b1][2] * W[b2][0]);
+        F[b][2] = dW[2][1] - dW[1][2] + gw * (W[b1][1] * W[b2][2] - W[b1][2] * W[b2][1]);
+        // d_j W^b_i enters kt W^{b-1}_i with -g W^{b+1}_j and kt W^{b+1}_i with +g W^{b-1}_j
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            ktW[b2][i] -= gw * (dW[i][0] * W[b1][0] + dW[i][1] * W[b1][1] + dW[i][2] * W[b1][2]);
+            ktW[b1][i] += gw * (dW[i][0] * W[b2][0] + dW[i][1] * W[b2][1] + dW[i][2] * W[b2][2]);
+        }
+    }
+    // -g sum_j (W^b_j F^c_ij - W^c_j F^b_ij) with F_ij antisymmetric
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int b = (a + 1) % 3, cc = (a + 2) % 3;
+        // i = x: j = y (F_xy), z (F_xz)
+        ktW[a][0] -= gw * ((W[b][1] * F[cc][0] - W[cc][1] * F[b][0]) + (W[b][2] * F[cc][1] - W[cc][2] * F[b][1]));
+        // i = y: j = x (F_yx = -F_xy), z (F_yz)
+        ktW[a][1] -= gw * ((W[cc][0] * F[b][0] - W[b][0] * F[cc][0]) + (W[b][2] * F[cc][2] - W[cc][2] * F[b][2]));
+        // i = z: j = x (F_zx = -F_xz), y (F_zy = -F_yz)
+        ktW[a][2] -= gw * ((W[cc][0] * F[b][1] - W[b][0] * F[cc][1]) + (W[cc][1] * F[b][2] - W[b][1] * F[cc][2]));
+    }
+    // auxiliary gradient
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        T gx, gy_, gz;
+        A.grad(16 + a, gx, gy_, gz);
+        ktW[a][0] -= gx;
+        ktW[a][1] -= gy_;
+        ktW[a][2] -= gz;
+    }
+
+    // ---- U(1) block (field_strengths.jl:281-311, main_rk4.jl:562-581)
+    T ktY[3], FY[3];
+    {
+        T dY[3][3], lap[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) A.grad_lap(13 + i, dY[i][0], dY[i][1], dY[i][2], lap[i]);
+        FY[0] = dY[1][0] - dY[0][1];
+        FY[1] = dY[2][0] - dY[0][2];
+        FY[2] = dY[2][1] - dY[1][2];
+        T gx, gy_, gz;
+        A.grad(19, gx, gy_, gz);
+        ktY[0] = lap[0] + jY[0] - gx;
+        ktY[1] = lap[1] + jY[1] - gy_;
+        ktY[2] = lap[2] + jY[2] - gz;
+    }
+
+    // ---- beta (CP-odd) terms
+    if (BETA) {
+        T Wt[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) Wt[a][i] = A.v(24 + 3 * a + i);
+        const T Yt2 = A.v(33), Yt3 = A.v(34), Yt4 = A.v(35);
+        // dual field strength: B_x = F_yz, B_y = -F_xz, B_z = F_xy
+        const T bWt = (Wt[0][0] * F[0][2] + Wt[0][1] * (-F[0][1]) + Wt[0][2] * F[0][0] +
+                       Wt[1][0] * F[1][2] + Wt[0][1] * (-F[1][1]) + Wt[0][2] * F[1][0] +
+                       Wt[2][0] * F[2][2] + Wt[0][1] * (-F[2][1]) + Wt[0][2] * F[2][0]);
+        const T bYt = (Yt2 * FY[2] + Yt3 * (-FY[1]) + Yt4 * FY[0]);
+        const T bsum = c.bW * bWt + c.bY * bYt;
+        ktp1 += bsum * p1;
+        ktp2 += bsum * p2;
+        ktp3 += bsum * p3;
+        ktp4 += bsum * p4;
+        const T bwp = c.bW2 * pdot, byp = c.bY2 * pdot;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            ktW[a][0] += -bwp * F[a][2] + c.bW2 * (cy * Wt[a][2] - cz * Wt[a][1]);
+            ktW[a][1] += bwp * F[a][1] + c.bW2 * (cz * Wt[a][0] - cx * Wt[a][2]);
+            ktW[a][2] += -bwp * F[a][0] + c.bW2 * (cx * Wt[a][1] - cy * Wt[a][0]);
+        }
+        ktY[0] += -byp * FY[2] + c.bY2 * (cy * Yt4 - cz * Yt3);
+        ktY[1] += byp * FY[1] + c.bY2 * (cz * Yt2 - cx * Yt4);
+        ktY[2] += -byp * FY[0] + c.bY2 * (cx * Yt3 - cy * Yt2);
+    }
+    out(20, ktp1);
+    out(21, ktp2);
+    out(22, ktp3);
+    out(23, ktp4);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) out(24 + 3 * a + i, ktW[a][i]);
+    out(33, ktY[0]);
+    out(34, ktY[1]);
+    out(35, ktY[2]);
+}

@@ -1,0 +1,291 @@
+// stage.cu -- fused RK4 stage kernels.
+//
+// One launch = one stage of classical RK4 (gpu-kernels-rk4/main_rk4.jl:
+// 6146-6437): the stage kernel rk4_step! (main_rk4.jl:52-661) with the
+// reference's broadcast combination fused into its epilogue, so the 144
+// broadcast kernels and ~72 temporary N^3 arrays of a reference step become
+// four launches and no temporaries.  The stage input X is written once per
+// stage by the previous launch; the periodic halo is a wrap of the neighbour
+// offsets inside the kernel (no ghost cells, no halo exchange).
+//
+// FP64 form (reference accumulation order, FMA contracted):
+//   stage 1: k = f(y);   yn = y  + k dt/6;  X2 = y + k dt/2
+//   stage 2: k = f(X2);  yn = yn + k dt/3;  X3 = y + k dt/2
+//   stage 3: k = f(X3);  yn = yn + k dt/3;  X4 = y + k dt
+//   stage 4: k = f(X4);  y  = yn + k dt/6
+// FP32 form (FP32 stencils and fluxes, compensated float hi/lo state):
+//   stage s < 4: k_s = f(X_s) stored as float, X_{s+1} = y_hi + c_s k_s
+//   stage 4:     (y_hi, y_lo) += dt/6 (k1 + 2 k2 + 2 k3 + k4), in place
+// (X_1 is y_hi itself).  Bytes per site-update: FP64 4608, FP32 2736.
+#include "ewpt_internal.cuh"
+
+namespace {
+
+constexpr int BX = 32, BY = 4;
+
+// Stage input read from global memory through the read-only path.
+template <typename TL, typename T>
+struct GlobalAcc {
+    const Ptr36& P;
+    int c;
+    int ox[6], oy[6], oz[6];
+    StencilCoef<T> s;
+
+    __device__ __forceinline__ T ld(int a, int off) const {
+        return (T)__ldg(reinterpret_cast<const TL*>(P.p[a]) + (c + off));
+    }
+    __device__ __forceinline__ T v(int a) const { return ld(a, 0); }
+    __device__ __forceinline__ T d1(int a, const int* o) const {
+        return s.a1 * (ld(a, o[0]) - ld(a, o[3])) + s.a2 * (ld(a, o[1]) - ld(a, o[4])) +
+               s.a3 * (ld(a, o[2]) - ld(a, o[5]));
+    }
+    __device__ __forceinline__ void grad(int a, T& gx, T& gy, T& gz) const {
+        gx = d1(a, ox);
+        gy = d1(a, oy);
+        gz = d1(a, oz);
+    }
+    __device__ __forceinline__ void grad_lap(int a, T& gx, T& gy, T& gz, T& lap) const {
+        T s1 = T(0), s2 = T(0), s3 = T(0);
+        {
+            const T p1 = ld(a, ox[0]), p2 = ld(a, ox[1]), p3 = ld(a, ox[2]);
+            const T m1 = ld(a, ox[3]), m2 = ld(a, ox[4]), m3 = ld(a, ox[5]);
+            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 = p1 + m1;
+            s2 = p2 + m2;
+            s3 = p3 + m3;
+        }
+        {
+            const T p1 = ld(a, oy[0]), p2 = ld(a, oy[1]), p3 = ld(a, oy[2]);
+            const T m1 = ld(a, oy[3]), m2 = ld(a, oy[4]), m3 = ld(a, oy[5]);
+            gy = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 += p1 + m1;
+            s2 += p2 + m2;
+            s3 += p3 + m3;
+        }
+        {
+            const T p1 = ld(a, oz[0]), p2 = ld(a, oz[1]), p3 = ld(a, oz[2]);
+            const T m1 = ld(a, oz[3]), m2 = ld(a, oz[4]), m3 = ld(a, oz[5]);
+            gz = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 += p1 + m1;
+            s2 += p2 + m2;
+            s3 += p3 + m3;
+        }
+        lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
+    }
+    __device__ __forceinline__ T div3(int a) const { return d1(a, ox) + d1(a + 1, oy) + d1(a + 2, oz); }
+};
+
+template <typename TL, typename T>
+__device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc, GlobalAcc<TL, T>& A) {
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return false;
+    A.c = i + g.nx * (j + g.ny * k);
+    axis_offsets(i, g.nx, 1, A.ox);
+    axis_offsets(j, g.ny, g.nx, A.oy);
+    axis_offsets(k, g.nz, g.nx * g.ny, A.oz);
+    A.s = sc;
+    return true;
+}
+
+// ------------------------------------------------------------- rk4_step!
+struct RatesSink {
+    const MPtr36& R;
+    int c;
+    __device__ __forceinline__ void operator()(int a, double r) const { reinterpret_cast<double*>(R.p[a])[c] = r; }
+};
+
+template <bool BETA>
+__global__ void __launch_bounds__(BX* BY) k_rates_fp64(Grid g, const __grid_constant__ Ptr36 X,
+                                                       const __grid_constant__ MPtr36 R, PhysCoef<double> pc,
+                                                       StencilCoef<double> sc) {
+    GlobalAcc<double, double> A{X};
+    if (!make_acc(g, sc, A)) return;
+    RatesSink out{R, A.c};
+    site_rates<double, BETA>(A, pc, out);
+}
+
+// ------------------------------------------------------------- FP64 stage
+template <int STAGE>
+struct Fp64Sink {
+    const GlobalAcc<double, double>& A;
+    const double* __restrict__ y;
+    double* yn;
+    double* __restrict__ xn;
+    double* acc_out;
+    int64_t S;
+    double w, h;
+    __device__ __forceinline__ void operator()(int a, double r) const {
+        const int64_t q = a * S + A.c;
+        if (STAGE == 1) {
+            const double ya = A.v(a);  // X1 == y
+            yn[q] = fma(r, w, ya);
+            xn[q] = fma(r, h, ya);
+        } else if (STAGE < 4) {
+            yn[q] = fma(r, w, yn[q]);
+            xn[q] = fma(r, h, __ldg(y + q));
+        } else {
+            acc_out[q] = fma(r, w, yn[q]);
+        }
+    }
+};
+
+template <int STAGE, bool BETA>
+__global__ void __launch_bounds__(BX* BY) k_stage_fp64(Grid g, const __grid_constant__ Ptr36 X,
+                                                       const double* __restrict__ y, double* yn,
+                                                       double* __restrict__ xn, double* acc_out,
+                                                       PhysCoef<double> pc, StencilCoef<double> sc, double w,
+                                                       double h) {
+    GlobalAcc<double, double> A{X};
+    if (!make_acc(g, sc, A)) return;
+    Fp64Sink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};
+    site_rates<double, BETA>(A, pc, out);
+}
+
+// ------------------------------------------------------------- FP32 stage
+// Compensated accumulation (hi, lo) += p (TwoSum, then renormalise).
+__device__ __forceinline__ void acc2(float& hi, float& lo, float p) {
+    const float s = hi + p;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (p - bp);
+    const float t = lo + e;
+    hi = s + t;
+    lo = t - (hi - s);
+}
+
+struct Fp32Bufs {
+    float* yhi;  // [36][S] state, high part (also the stage-1 stencil input)
+    float* ylo;  // [36][S] state, low part
+    float* k1;   // [36][S] stage rates
+    float* k2;
+    float* k3;
+};
+
+template <int STAGE>
+struct Fp32Sink {
+    const GlobalAcc<float, float>& A;
+    Fp32Bufs b;
+    float* __restrict__ xn;
+    int64_t S;
+    float h, w6;
+    __device__ __forceinline__ void operator()(int a, float r) const {
+        const int64_t q = a * S + A.c;
+        if (STAGE == 1) {
+            b.k1[q] = r;
+            xn[q] = A.v(a) + h * r;  // X1 == y_hi
+        } else if (STAGE < 4) {
+            (STAGE == 2 ? b.k2 : b.k3)[q] = r;
+            xn[q] = __ldg(b.yhi + q) + h * r;
+        } else {
+            const float s = (b.k1[q] + r) + 2.f * (b.k2[q] + b.k3[q]);
+            float hi = b.yhi[q], lo = b.ylo[q];
+            acc2(hi, lo, w6 * s);
+            b.yhi[q] = hi;
+            b.ylo[q] = lo;
+        }
+    }
+};
+
+template <int STAGE, bool BETA>
+__global__ void __launch_bounds__(BX* BY) k_stage_fp32(Grid g, const __grid_constant__ Ptr36 X, Fp32Bufs b,
+                                                       float* __restrict__ xn, PhysCoef<float> pc,
+                                                       StencilCoef<float> sc, float h, float w6) {
+    GlobalAcc<float, float> A{X};
+    if (!make_acc(g, sc, A)) return;
+    Fp32Sink<STAGE> out{A, b, xn, g.S, h, w6};
+    site_rates<float, BETA>(A, pc, out);
+}
+
+__global__ void k_split(int64_t n, const double* __restrict__ src, float* __restrict__ hi, float* __restrict__ lo) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double v = src[q];
+        const float h = (float)v;
+        hi[q] = h;
+        lo[q] = (float)(v - (double)h);
+    }
+}
+
+__global__ void k_join(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+                       double* __restrict__ dst) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        dst[q] = (double)hi[q] + (double)lo[q];
+}
+
+inline dim3 grid_of(const Grid& g) { return dim3((g.nx + BX - 1) / BX, (g.ny + BY - 1) / BY, g.nz); }
+
+Ptr36 pack(const void* base, int64_t S, size_t elem) {
+    Ptr36 P;
+    for (int a = 0; a < 36; ++a) P.p[a] = static_cast<const char*>(base) + (size_t)a * S * elem;
+    return P;
+}
+
+}  // namespace
+
+cudaError_t launch_rates_fp64(const Grid& g, const Ptr36& in, const MPtr36& out, const ewpt_params& p,
+                              double Jex, double gam, cudaStream_t st) {
+    const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
+    const StencilCoef<double> sc = make_stencil<double>(p.dx);
+    const bool beta = p.beta_w != 0.0 || p.beta_y != 0.0;
+    if (beta)
+        k_rates_fp64<true><<<grid_of(g), dim3(BX, BY), 0, st>>>(g, in, out, pc, sc);
+    else
+        k_rates_fp64<false><<<grid_of(g), dim3(BX, BY), 0, st>>>(g, in, out, pc, sc);
+    return cudaGetLastError();
+}
+
+template <bool BETA>
+static void step_fp64(const Grid& g, double* y, double* yn, double* xa, double* xb, const PhysCoef<double>& pc,
+                      const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+    const dim3 gr = grid_of(g), bl(BX, BY);
+    k_stage_fp64<1, BETA><<<gr, bl, 0, st>>>(g, pack(y, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 6., dt / 2.);
+    k_stage_fp64<2, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.);
+    k_stage_fp64<3, BETA><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 3., dt);
+    k_stage_fp64<4, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
+}
+
+cudaError_t launch_step_fp64(const Grid& g, double* y, double* yn, double* xa, double* xb, const ewpt_params& p,
+                             double Jex, double gam, cudaStream_t st) {
+    const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
+    const StencilCoef<double> sc = make_stencil<double>(p.dx);
+    if (p.beta_w != 0.0 || p.beta_y != 0.0)
+        step_fp64<true>(g, y, yn, xa, xb, pc, sc, p.dt, st);
+    else
+        step_fp64<false>(g, y, yn, xa, xb, pc, sc, p.dt, st);
+    return cudaGetLastError();
+}
+
+// FP32 form.  yn.hi/yn.lo/xb are reused as the k1/k2/k3 stores; xa and
+// the second half of the k buffers hold the two stage-input ping-pong arrays.
+template <bool BETA>
+static void step_fp32(const Grid& g, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
+                      const StencilCoef<float>& sc, double dt, cudaStream_t st) {
+    const dim3 gr = grid_of(g), bl(BX, BY);
+    const float h2 = (float)(dt / 2.), h1 = (float)dt, w6 = (float)(dt / 6.);
+    k_stage_fp32<1, BETA><<<gr, bl, 0, st>>>(g, pack(b.yhi, g.S, 4), b, xa, pc, sc, h2, w6);
+    k_stage_fp32<2, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, xb, pc, sc, h2, w6);
+    k_stage_fp32<3, BETA><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 4), b, xa, pc, sc, h1, w6);
+    k_stage_fp32<4, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, nullptr, pc, sc, 0.f, w6);
+}
+
+cudaError_t launch_step_fp32(const Grid& g, Fp32State y, Fp32Work w, const ewpt_params& p, double Jex, double gam,
+                             cudaStream_t st) {
+    const PhysCoef<float> pc = make_phys<float>(p, Jex, gam);
+    const StencilCoef<float> sc = make_stencil<float>(p.dx);
+    Fp32Bufs b{y.hi, y.lo, w.k1, w.k2, w.k3};
+    if (p.beta_w != 0.0 || p.beta_y != 0.0)
+        step_fp32<true>(g, b, w.xa, w.xb, pc, sc, p.dt, st);
+    else
+        step_fp32<false>(g, b, w.xa, w.xb, pc, sc, p.dt, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp32_split(const Grid& g, const double* src, Fp32State dst, cudaStream_t st) {
+    k_split<<<1216, 256, 0, st>>>(36 * g.S, src, dst.hi, dst.lo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp32_join(const Grid& g, Fp32State src, double* dst, cudaStream_t st) {
+    k_join<<<1216, 256, 0, st>>>(36 * g.S, src.hi, src.lo, dst);
+    return cudaGetLastError();
+}

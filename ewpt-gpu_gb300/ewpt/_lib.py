@@ -1,0 +1,97 @@
+"""ctypes binding of libewpt.so (include/ewpt.h).
+
+The library is built in-tree by ewpt-gpu_gb300/build_lib.py (nvcc, sm_103a).
+Loading fails loudly when it has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(ROOT, "build", "libewpt.so")
+HEADER = os.path.join(os.path.dirname(ROOT), "include", "ewpt.h")
+
+NARR = 36
+NDIAG = 20
+
+OK, ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_STATE = range(8)
+FP64, FP32 = 0, 1
+FIELD_B, FIELD_B2, FIELD_HIGGS = 0, 1, 2
+SPEC_LOG, SPEC_UNIQUE = 0, 1
+
+
+class EwptParams(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("precision", C.c_int32),
+                ("dx", C.c_double), ("dt", C.c_double),
+                ("gw", C.c_double), ("gy", C.c_double), ("gp2", C.c_double),
+                ("lam", C.c_double), ("vev", C.c_double), ("theta_w", C.c_double),
+                ("beta_w", C.c_double), ("beta_y", C.c_double), ("gamma_inp", C.c_double),
+                ("mH", C.c_double), ("t_sat", C.c_double),
+                ("thermal_init", C.c_int32), ("device", C.c_int32)]
+
+
+class EwptError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+DP = C.POINTER(C.c_double)
+DPA = DP * NARR
+
+
+def _sig(L):
+    P = C.POINTER(EwptParams)
+    V = C.c_void_p
+    L.ewpt_params_default.argtypes = [P, C.c_int32]
+    L.ewpt_create.argtypes = [P, C.POINTER(V)]
+    L.ewpt_destroy.argtypes = [V]
+    L.ewpt_last_error.argtypes = [V]
+    L.ewpt_last_error.restype = C.c_char_p
+    L.ewpt_set_state.argtypes = [V, DPA, C.c_int32]
+    L.ewpt_get_state.argtypes = [V, DPA, C.c_int32]
+    L.ewpt_set_state_packed.argtypes = [V, C.c_void_p, C.c_int32]
+    L.ewpt_get_state_packed.argtypes = [V, C.c_void_p, C.c_int32]
+    L.ewpt_step.argtypes = [V, C.c_int32]
+    L.ewpt_step_explicit.argtypes = [V, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_iteration.argtypes = [V]
+    L.ewpt_iteration.restype = C.c_int64
+    L.ewpt_sync.argtypes = [V]
+    L.ewpt_stream.argtypes = [V]
+    L.ewpt_stream.restype = C.c_void_p
+    L.ewpt_rk4_rates.argtypes = [P, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
+    L.ewpt_diagnostics.argtypes = [V, DP]
+    L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
+    L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_kc_bin_nums.restype = C.c_int64
+
+
+def load():
+    """The loaded libewpt (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libewpt.so not built ({LIB_PATH}); run ewpt-gpu_gb300/build_lib.py "
+                               "(or __graft_entry__.build()) first")
+        L = C.CDLL(LIB_PATH)
+        _sig(L)
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    """Names of the functions declared in include/ewpt.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ewpt_\w+)\s*\(", txt)))
+
+
+def check(rc: int, ctx=None):
+    if rc != OK:
+        msg = load().ewpt_last_error(ctx).decode()
+        raise EwptError(rc, msg)
+    return rc

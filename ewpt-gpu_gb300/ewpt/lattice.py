@@ -1,0 +1,124 @@
+"""Host-side handle of one lattice context of libewpt.
+
+This is the Python mirror of the reference driver's data path: the 36 CuArrays
+of run() (gpu-kernels-rk4/main_rk4.jl:5178-5304) become one device context,
+`@cuda rk4_step!` + broadcasts (:6146-6437) become `step()`, the compute_*!
+kernels + host sums (:6451-6805) become `diagnostics()`, and fft + convolve_1d
+(:6580-6685, spec_routines.jl:47-77) become `spectrum()`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .params import Params
+
+DIAG_NAMES = ["PE", "KE", "GE", "EEW", "MEW", "EEY", "MEY", "EB", "EB2", "min_phi", "zero", "mean_phi",
+              "helicity", "total", "gauss_W", "gauss_W_max", "gauss_Y", "gauss_Y_max", "aux_W", "aux_Y"]
+
+FIELDS = {"B": _lib.FIELD_B, "B2": _lib.FIELD_B2, "higgs": _lib.FIELD_HIGGS}
+MODES = {"log": _lib.SPEC_LOG, "unique": _lib.SPEC_UNIQUE}
+
+
+class Lattice:
+    def __init__(self, params: Params):
+        self.params = params
+        self.L = _lib.load()
+        self._cp = params.to_c()
+        h = C.c_void_p()
+        _lib.check(self.L.ewpt_create(C.byref(self._cp), C.byref(h)))
+        self.h = h
+        self.S = params.sites
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if self.h:
+            self.L.ewpt_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        return _lib.check(rc, self.h)
+
+    # ------------------------------------------------------------ state I/O
+    def set_state(self, y: np.ndarray):
+        """y: float64 array (36, S) on the host."""
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        if y.shape != (36, self.S):
+            raise ValueError(f"state must have shape (36, {self.S})")
+        self._chk(self.L.ewpt_set_state_packed(self.h, y.ctypes.data, 0))
+
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((36, self.S))
+        self._chk(self.L.ewpt_get_state_packed(self.h, out.ctypes.data, 0))
+        return out
+
+    def set_state_device(self, ptr: int):
+        """ptr: device address of 36*S contiguous doubles."""
+        self._chk(self.L.ewpt_set_state_packed(self.h, C.c_void_p(ptr), 1))
+
+    def get_state_device(self, ptr: int):
+        self._chk(self.L.ewpt_get_state_packed(self.h, C.c_void_p(ptr), 1))
+
+    # ------------------------------------------------------------ stepping
+    def step(self, n: int = 1, Jex: float | None = None, gamma: float | None = None):
+        if Jex is None and gamma is None:
+            self._chk(self.L.ewpt_step(self.h, int(n)))
+        else:
+            self._chk(self.L.ewpt_step_explicit(self.h, int(n), float(Jex or 0.0), float(gamma or 0.0)))
+
+    def sync(self):
+        self._chk(self.L.ewpt_sync(self.h))
+
+    @property
+    def iteration(self) -> int:
+        return int(self.L.ewpt_iteration(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.ewpt_stream(self.h) or 0)
+
+    # ------------------------------------------------------------ observables
+    def diagnostics(self, allow_nonfinite: bool = False) -> np.ndarray:
+        out = np.zeros(_lib.NDIAG)
+        rc = self.L.ewpt_diagnostics(self.h, out.ctypes.data_as(_lib.DP))
+        if rc == _lib.ERR_NONFINITE and allow_nonfinite:
+            return out
+        self._chk(rc)
+        return out
+
+    def spectrum(self, field: str = "B", mode: str = "log", nbins: int = 40) -> dict:
+        k, s, c, m = (np.zeros(nbins) for _ in range(4))
+        nout = C.c_int32(0)
+        self._chk(self.L.ewpt_spectrum(self.h, FIELDS[field], MODES[mode], int(nbins),
+                                       k.ctypes.data_as(_lib.DP), s.ctypes.data_as(_lib.DP),
+                                       c.ctypes.data_as(_lib.DP), m.ctypes.data_as(_lib.DP), C.byref(nout)))
+        n = nout.value
+        return dict(k=k[:n], sum=s[:n], count=c[:n], mean=m[:n])
+
+
+def rk4_rates_device(params: Params, in_ptrs, out_ptrs, Jex: float = 0.0, gamma: float = 0.0, stream: int = 0):
+    """One rk4_step! launch on device arrays (36 input and 36 output addresses)."""
+    L = _lib.load()
+    cp = params.to_c()
+    ia = (C.c_void_p * 36)(*[C.c_void_p(int(p)) for p in in_ptrs])
+    oa = (C.c_void_p * 36)(*[C.c_void_p(int(p)) for p in out_ptrs])
+    _lib.check(L.ewpt_rk4_rates(C.byref(cp), ia, oa, float(Jex), float(gamma), C.c_void_p(stream)))
+
+
+def kc_bin_nums(cx: int, cy: int, cz: int) -> int:
+    return int(_lib.load().ewpt_kc_bin_nums(cx, cy, cz))

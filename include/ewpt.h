@@ -1,0 +1,159 @@
+/*
+ * ewpt.h -- C ABI of libewpt, the GB300 (sm_103a) implementation of the
+ * real-time RK4 lattice evolution of the electroweak bosonic sector of
+ * Teerthal/EWPT-GPU.
+ *
+ * Plain C types only (no CUDA or torch types): a Julia `ccall`, Python
+ * `ctypes` or C caller binds these directly.  Every entry point returns an
+ * int status (EWPT_OK = 0); the message of the last failure is returned by
+ * ewpt_last_error().
+ *
+ * Array order.  The state is 36 real arrays of nx*ny*nz doubles, each in
+ * Julia column-major order (linear index i + nx*(j + ny*k), x fastest), i.e.
+ * exactly the memory of a CuArray{Float64,3}.  Order of the 36 arrays:
+ *    0- 3  phi_1..phi_4                  (Higgs doublet, 4 real components)
+ *    4-12  W_1_2 W_1_3 W_1_4  W_2_2 .. W_3_4   (W^a_i, a = 1..3, i = x,y,z)
+ *   13-15  Y_2 Y_3 Y_4                   (hypercharge)
+ *   16-18  Gamma_1..Gamma_3, 19 Sigma    (Gauss-constraint auxiliaries)
+ *   20-23  dphi_a_dt, 24-32 dW_a_i_dt, 33-35 dY_i_dt   (momenta)
+ * The rates ("k" and "kt" arrays of rk4_step!) use the same order: rate a
+ * is d/dt of array a.
+ *
+ * Threading: one context is bound to one CUDA stream and must be used from
+ * one host thread at a time; distinct contexts are independent.
+ */
+#ifndef EWPT_H
+#define EWPT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EWPT_NARR 36
+#define EWPT_NDIAG 20
+
+enum ewpt_status {
+    EWPT_OK = 0,
+    EWPT_ERR_ARG = 1,       /* invalid argument (dims, null pointer, non-finite parameter) */
+    EWPT_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    EWPT_ERR_CUFFT = 3,     /* a cuFFT call failed */
+    EWPT_ERR_OOM = 4,       /* device allocation failed */
+    EWPT_ERR_NONFINITE = 5, /* the state holds NaN/Inf */
+    EWPT_ERR_TIMEOUT = 6,   /* a bounded device-side wait ran out */
+    EWPT_ERR_STATE = 7      /* call not valid in the context's current state */
+};
+
+enum ewpt_precision {
+    EWPT_FP64 = 0, /* stencils, fluxes, state and reductions in FP64 */
+    EWPT_FP32 = 1  /* FP32 stencils and fluxes; compensated FP32 hi/lo RK4 state; FP64 reductions */
+};
+
+/* Parameter set.  Mirrors gpu-kernels-rk4/parameters.jl:1-98 (couplings,
+ * lattice, dt = dx/ARG5, damping gamma_inp, beta_W/beta_Y, mH, t_sat) plus
+ * the run() switch thermal_init (main_rk4.jl:7082) that enables the
+ * J_ext/damp schedule of main_rk4.jl:5154-5172. */
+typedef struct ewpt_params {
+    int32_t nx, ny, nz;   /* lattice sites per axis, each >= 7 (parameters.jl:14) */
+    int32_t precision;    /* enum ewpt_precision */
+    double dx, dt;        /* parameters.jl:22-23 */
+    double gw, gy, gp2;   /* parameters.jl:16-19 */
+    double lambda, vev;   /* parameters.jl:20-21 */
+    double theta_w;       /* Weinberg angle used by the B field, parameters.jl:17,26 */
+    double beta_w, beta_y;/* CP-odd couplings, parameters.jl:34-35 */
+    double gamma_inp;     /* damping after t_sat, parameters.jl:29 */
+    double mH, t_sat;     /* J_ext/damp schedule, parameters.jl:24,40 */
+    int32_t thermal_init; /* 1: apply J_ext/damp schedule (main_rk4.jl:5154-5172) */
+    int32_t device;       /* CUDA device ordinal */
+} ewpt_params;
+
+typedef struct ewpt_ctx ewpt_ctx;
+
+/* Fills p with the reference's defaults (parameters.jl) for an n^3 lattice:
+ * gw = 0.65, gy = gw*tan(asin(sqrt(0.22))), gp2 = 0.99, lambda = 0.129,
+ * vev = 1, dx = 0.25, dt = dx/10, mH = 2*sqrt(lambda)*vev, t_sat = 2. */
+int ewpt_params_default(ewpt_params* p, int32_t n);
+
+/* Allocates the device state of one lattice (replaces the CuArray
+ * allocations of main_rk4.jl:5178-5304).  State starts at zero. */
+int ewpt_create(const ewpt_params* p, ewpt_ctx** out);
+int ewpt_destroy(ewpt_ctx* ctx);
+
+/* Message of the last failure on ctx (ctx may be NULL: last failure of any
+ * call that had no context).  Never NULL. */
+const char* ewpt_last_error(const ewpt_ctx* ctx);
+
+/* Copy the 36 state arrays in (set) or out (get).  arrays[a] points to
+ * nx*ny*nz doubles on the host (on_device = 0) or on the context's device
+ * (on_device = 1).  Replaces copyto!(CuArray, Array) / Array(CuArray). */
+int ewpt_set_state(ewpt_ctx* ctx, const double* const arrays[EWPT_NARR], int32_t on_device);
+int ewpt_get_state(ewpt_ctx* ctx, double* const arrays[EWPT_NARR], int32_t on_device);
+/* Same with one packed buffer of 36*nx*ny*nz doubles (array-major). */
+int ewpt_set_state_packed(ewpt_ctx* ctx, const double* buf, int32_t on_device);
+int ewpt_get_state_packed(ewpt_ctx* ctx, double* buf, int32_t on_device);
+
+/* nsteps classical RK4 steps (main_rk4.jl:6146-6437), asynchronous on the
+ * context's stream.  Iteration it (1-based, counted by the context) uses
+ * Jex = J_ext(it) and gamma = damp(it) (main_rk4.jl:5154-5172). */
+int ewpt_step(ewpt_ctx* ctx, int32_t nsteps);
+/* Same with explicit Jex and gamma for every step (counter still advances). */
+int ewpt_step_explicit(ewpt_ctx* ctx, int32_t nsteps, double Jex, double gamma);
+/* Iterations done so far (the `it` of the reference loop). */
+int64_t ewpt_iteration(const ewpt_ctx* ctx);
+/* Wait for all work queued on the context. */
+int ewpt_sync(ewpt_ctx* ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void* ewpt_stream(ewpt_ctx* ctx);
+
+/* Drop-in for one launch of rk4_step! (main_rk4.jl:52-661, launched at
+ * :6155/:6226/:6298/:6370): reads the 20 fields + 16 momenta in[0..35]
+ * (device pointers) and writes the 20 k + 16 kt rates out[0..35] (device
+ * pointers), FP64, asynchronously on `stream` (a cudaStream_t or NULL).
+ * in and out must not alias. */
+int ewpt_rk4_rates(const ewpt_params* p, const double* const in[EWPT_NARR],
+                   double* const out[EWPT_NARR], double Jex, double gamma, void* stream);
+
+/* Snapshot diagnostics of the current state, FP64, one fused reduction
+ * (replaces compute_PE!..compute_Az! + host sums, main_rk4.jl:6451-6805):
+ *   out[0..6]  PE KE GE EEW MEW EEY MEY   (sum * dx^3; columns 1-7 of
+ *              total_energies, main_rk4.jl:6790-6796)
+ *   out[7]     0.5*sum(B^2)*dx^3          out[8]  0.5*sum(B_2^2)*dx^3
+ *   out[9]     min |Phi|                  out[10] 0
+ *   out[11]    mean |Phi|                 out[12] sum(B_2 . A)*dx^3
+ *   out[13]    total energy = sum of out[0..6]  (main_rk4.jl:6921)
+ *   out[14]    sqrt(sum_a sum G_a^2 dx^3), G_a = d_i E^a_i - rho^a (SU(2) Gauss law)
+ *   out[15]    max |G_a|    out[16] sqrt(sum G_Y^2 dx^3)   out[17] max |G_Y|
+ *   out[18]    sqrt(sum_a sum (Gamma_a - d_i W^a_i)^2 dx^3)
+ *   out[19]    sqrt(sum (Sigma - d_i Y_i)^2 dx^3)
+ * Synchronous.  Returns EWPT_ERR_NONFINITE (row still written) if any
+ * column is NaN/Inf. */
+int ewpt_diagnostics(ewpt_ctx* ctx, double out[EWPT_NDIAG]);
+
+enum ewpt_field { EWPT_FIELD_B = 0, EWPT_FIELD_B2 = 1, EWPT_FIELD_HIGGS = 2 };
+enum ewpt_spec_mode { EWPT_SPEC_LOG = 0, EWPT_SPEC_UNIQUE = 1 };
+
+/* Power spectrum of the current state (replaces fft(E_t) + convolve_1d,
+ * main_rk4.jl:6580-6685 and spec_routines.jl:47-77).  P(n) = sum over the
+ * components of |FFT(component)|^2 (unnormalised forward transform), FFT of
+ *   EWPT_FIELD_B      B_x, B_y, B_z   (compute_Bx/By/Bz!, main_rk4.jl:2303-2822)
+ *   EWPT_FIELD_B2     B_2 components  (compute_B_2_*!, main_rk4.jl:3718-4250)
+ *   EWPT_FIELD_HIGGS  phi_1..phi_4 (DC mode removed).
+ * mode EWPT_SPEC_LOG: nbins (<= 256) shells log-uniform in |n| over
+ * [1, min(nx,ny,nz)/2], DC excluded; k[b] = geometric shell centre.
+ * mode EWPT_SPEC_UNIQUE: one bin per distinct integer |n| in increasing
+ * order, the first nbins of them (convolve_1d with
+ * nbins = ewpt_kc_bin_nums(cut)); k[b] = |n|.
+ * Writes sum, count (modes), mean = sum/count per bin; *nbins_out (may be
+ * NULL) = bins written.  Synchronous. */
+int ewpt_spectrum(ewpt_ctx* ctx, int32_t field, int32_t mode, int32_t nbins, double* k, double* sum,
+                  double* count, double* mean, int32_t* nbins_out);
+
+/* Number of distinct |K| on a cx*cy*cz index lattice (Kc_bin_nums,
+ * spec_routines.jl:32-43), -1 on bad input. */
+int64_t ewpt_kc_bin_nums(int32_t cx, int32_t cy, int32_t cz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EWPT_H */

@@ -778,16 +778,36 @@ int64_t or_convolve_1d(const or_params* p, const double* P, int cx, int cy, int 
     return b;
 }
 
-/* Log-spaced shell spectrum: nshell shells with edges log-uniform in |n| over
- * [1, nmax] (nmax = min(nx,ny,nz)/2), DC excluded, |n| >= nmax folded into the
- * last shell only if |n| <= nmax.  Outputs per-shell sum, count and mean. */
+/* Integer |n|^2 thresholds of nshell log-spaced shells over |n| in [1, nmax]:
+ * mode m = |n|^2 is in shell b when thr[b] <= m < thr[b+1]; thr[0] = 1,
+ * thr[nshell] = nmax^2 + 1.  thr[b] is the smallest m with sqrt(m) >= e_b,
+ * e_b = exp(log(nmax) b / nshell). */
+void or_shell_thresholds(int nmax, int nshell, int64_t* thr) {
+    const double lmax = log((double)nmax);
+    for (int b = 0; b <= nshell; ++b) {
+        if (b == 0) { thr[b] = 1; continue; }
+        if (b == nshell) { thr[b] = (int64_t)nmax * nmax + 1; continue; }
+        const double e = exp(lmax * (double)b / (double)nshell);
+        int64_t m = (int64_t)ceil(e * e);
+        while (m > 1 && sqrt((double)(m - 1)) >= e) --m;
+        while (sqrt((double)m) < e) ++m;
+        thr[b] = m;
+    }
+}
+
+/* Log-spaced shell spectrum over the full lattice: nshell shells in |n| over
+ * [1, nmax], nmax = min(nx,ny,nz)/2, DC and |n| > nmax excluded.  Outputs
+ * per-shell sum, count, mean and the geometric shell centre. */
 int or_shell_spectrum(const or_params* p, const double* P, int nshell,
                       double* ssum, double* scount, double* smean, double* kcenter) {
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     int nm = nx < ny ? nx : ny;
     nm = nm < nz ? nm : nz;
-    const double nmax = (double)(nm / 2);
-    const double lmax = log(nmax);
+    const int nmax = nm / 2;
+    int64_t* thr = (int64_t*)malloc(sizeof(int64_t) * (nshell + 1));
+    if (!thr) return 2;
+    or_shell_thresholds(nmax, nshell, thr);
+    const double lmax = log((double)nmax);
     for (int b = 0; b < nshell; ++b) {
         ssum[b] = 0; scount[b] = 0; smean[b] = 0;
         kcenter[b] = exp(lmax * (b + 0.5) / nshell);
@@ -796,16 +816,14 @@ int or_shell_spectrum(const or_params* p, const double* P, int nshell,
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
                 const int64_t m = kc2(i, nx) + kc2(j, ny) + kc2(k, nz);
-                if (m == 0) continue;
-                const double r = sqrt((double)m);
-                if (r > nmax) continue;
-                int b = (int)floor(log(r) / lmax * nshell);
-                if (b >= nshell) b = nshell - 1;
-                if (b < 0) b = 0;
+                if (m == 0 || m >= thr[nshell]) continue;
+                int b = 0;
+                while (b + 1 < nshell && thr[b + 1] <= m) ++b;
                 ssum[b] += P[i + (int64_t)nx * (j + (int64_t)ny * k)];
                 scount[b] += 1;
             }
     for (int b = 0; b < nshell; ++b) smean[b] = scount[b] > 0 ? ssum[b] / scount[b] : 0.0;
+    free(thr);
     return 0;
 }
 

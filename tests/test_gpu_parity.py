@@ -1,0 +1,204 @@
+"""GPU parity: libewpt (through its C ABI) against the CPU oracle and the
+golden vectors of the reference's own kernel source.
+
+Tolerances.  FP64 work is not bit-exact (the GPU path uses FMA and
+pre-divided stencil coefficients where the reference divides): per array,
+max |gpu - ref| <= tol * max |ref| with tol = 1e-12 for one rate evaluation
+and 1e-11 after 100 RK4 steps (the FP64 parity bar); diagnostics 1e-10
+relative; spectra 1e-10 relative per shell.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ewpt
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import build_lib
+
+    build_lib.build()
+    orc.build()
+
+
+def rel_err(a, b):
+    scale = np.maximum(np.abs(b).max(axis=-1), 1e-300)
+    return (np.abs(a - b).max(axis=-1) / scale).max()
+
+
+def oparams(p: ewpt.Params):
+    return orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
+
+
+def golden(golden_dir, name):
+    return dict(np.load(os.path.join(golden_dir, f"ref_{name}.npz")))
+
+
+def params_from_golden(g, **over):
+    shape = tuple(int(v) for v in g["shape"])
+    return ewpt.Params(shape=shape, N=shape[0], dx=float(g["p_dx"]), dt=float(g["dt"]), gw=float(g["p_gw"]),
+                       gy=float(g["p_gy"]), gp2=float(g["p_gp2"]), lam=float(g["p_lambda"]),
+                       vev=float(g["p_vev"]), beta_w=float(g["p_beta_w"]), beta_y=float(g["p_beta_y"]),
+                       theta_w=float(g["p_theta_w"]), **over)
+
+
+def perturbed_bubbles(shape, dx, nb, seed, amp=0.05):
+    y = ewpt.ic.bubbles_tanh(shape, dx, nb, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    y[4:] += amp * rng.normal(size=y[4:].shape)  # gauge fields, aux and momenta non-zero
+    return y
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_rk4_rates_dropin_matches_golden(golden_dir, case):
+    import torch
+
+    g = golden(golden_dir, case)
+    p = params_from_golden(g)
+    yin = torch.tensor(g["y0"], device="cuda:0", dtype=torch.float64).contiguous()
+    out = torch.zeros_like(yin)
+    ewpt.rk4_rates_device(p, [yin[a].data_ptr() for a in range(36)], [out[a].data_ptr() for a in range(36)],
+                          float(g["Jex"]), float(g["gam"]), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    r = out.cpu().numpy()
+    assert rel_err(r, g["rates"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_one_step_matches_golden(golden_dir, case):
+    g = golden(golden_dir, case)
+    p = params_from_golden(g)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(g["y0"])
+        lat.step(1, Jex=float(g["Jex"]), gamma=float(g["gam"]))
+        y1 = lat.get_state()
+    assert rel_err(y1, g["y1"]) < 1e-12
+
+
+@pytest.mark.parametrize("shape,beta", [((20, 24, 16), True), ((32, 32, 32), False)])
+def test_fp64_100_steps_vs_oracle(shape, beta):
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025,
+                                beta_w=0.3 if beta else 0.0, beta_y=0.2 if beta else 0.0)
+    y0 = perturbed_bubbles(shape, p.dx, 4, seed=11)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        lat.step(100, Jex=0.02, gamma=0.01)
+        y = lat.get_state()
+    yo = orc.rk4_step(oparams(p), y0, p.dt, 0.02, 0.01, nsteps=100)
+    assert np.isfinite(y).all()
+    assert rel_err(y, yo) < 1e-11
+
+
+def test_step_schedule_jext_damp():
+    """ewpt_step applies J_ext/damp per iteration (main_rk4.jl:5154-5172)."""
+    shape = (16, 16, 16)
+    p = ewpt.baseline_couplings(shape=shape, N=16, dx=0.25, dt=0.05, thermal_init=True, gamma_inp=0.3,
+                                mH=2.0 * np.sqrt(0.129))
+    p.t_sat = 0.5  # it*dt*mH crosses t_sat at it ~ 14, inside the 30 steps
+    y0 = perturbed_bubbles(shape, p.dx, 2, seed=3)
+    op = oparams(p)
+    yo = y0.copy()
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        lat.step(30)
+        y = lat.get_state()
+        assert lat.iteration == 30
+    for it in range(1, 31):
+        J = orc.jext(it, p.dt, p.mH, p.t_sat, True)
+        G = orc.damp(it, p.dt, p.mH, p.t_sat, True, p.gamma_inp)
+        yo = orc.rk4_step(op, yo, p.dt, J, G)
+    assert rel_err(y, yo) < 1e-11
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (20, 18, 22)])
+def test_diagnostics_vs_oracle(shape):
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025)
+    y0 = perturbed_bubbles(shape, p.dx, 3, seed=7, amp=0.2)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        d = lat.diagnostics()
+    do = orc.diagnostics(oparams(p), y0)
+    np.testing.assert_allclose(d, do, rtol=1e-10, atol=1e-13)
+
+
+def test_diagnostics_match_golden_row(golden_dir):
+    g = golden(golden_dir, "a")
+    p = params_from_golden(g)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(g["y0"])
+        d = lat.diagnostics()
+    np.testing.assert_allclose(d[:14], g["row"], rtol=1e-10)
+
+
+def _oracle_power(p, y, field):
+    den = orc.densities(oparams(p), y)
+    if field == "B":
+        comps = [den[7], den[8], den[9]]
+    elif field == "B2":
+        comps = [den[10], den[11], den[12]]
+    else:
+        comps = [y[a] - y[a].mean() for a in range(4)]
+    P = np.zeros(y.shape[1])
+    for f in comps:
+        F = np.fft.fftn(f.reshape(p.dims[::-1]))
+        P += (np.abs(F) ** 2).ravel()
+    return P
+
+
+@pytest.mark.parametrize("field", ["B", "B2", "higgs"])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (18, 16, 20)])
+def test_spectrum_log_shells_vs_oracle(field, shape):
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025)
+    y0 = perturbed_bubbles(shape, p.dx, 3, seed=9, amp=0.2)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        s = lat.spectrum(field, "log", 12)
+    ref = orc.shell_spectrum(oparams(p), _oracle_power(p, y0, field), 12)
+    np.testing.assert_array_equal(s["count"], ref["count"])
+    np.testing.assert_allclose(s["sum"], ref["sum"], rtol=1e-10)
+    np.testing.assert_allclose(s["mean"], ref["mean"], rtol=1e-10)
+
+
+def test_spectrum_unique_matches_convolve_1d_golden(golden_dir):
+    g = golden(golden_dir, "a")
+    p = params_from_golden(g)
+    cut = tuple(int(v) for v in g["cut"])
+    nb = ewpt.kc_bin_nums(*cut)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(g["y0"])
+        s = lat.spectrum("B", "unique", nb)
+    np.testing.assert_array_equal(s["k"], g["spec"][:, 0])
+    np.testing.assert_allclose(s["mean"], g["spec"][:, 1], rtol=1e-10)
+
+
+def test_fp32_form_tracks_fp64():
+    """FP32 form vs FP64 on a smooth bubble IC: fields within 1e-4 of FP64
+    after 100 steps, energy drift and Gauss violation within 2x of FP64
+    (plus a floor at FP32 round-off of the total energy), B spectrum 1e-4."""
+    shape = (32, 32, 32)
+    p64 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025)
+    p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32)
+    y0 = ewpt.ic.bubbles_tanh(shape, p64.dx, 4, seed=21)
+    res = {}
+    for name, p in (("64", p64), ("32", p32)):
+        with ewpt.Lattice(p) as lat:
+            lat.set_state(y0)
+            d0 = lat.diagnostics()
+            lat.step(100)
+            res[name] = (lat.get_state(), d0, lat.diagnostics(), lat.spectrum("B", "log", 12))
+    y64, y32 = res["64"][0], res["32"][0]
+    assert rel_err(y32[:20], y64[:20]) < 1e-4
+    e0 = res["64"][1][13]
+    drift64 = abs(res["64"][2][13] - e0)
+    drift32 = abs(res["32"][2][13] - e0)
+    assert drift32 <= 2.0 * drift64 + 1e-6 * abs(e0)
+    g64, g32 = res["64"][2][14], res["32"][2][14]
+    assert g32 <= 2.0 * g64 + 1e-6
+    s64, s32 = res["64"][3]["mean"], res["32"][3]["mean"]
+    m = s64 > 1e-12 * s64.max()
+    np.testing.assert_allclose(s32[m], s64[m], rtol=1e-4)

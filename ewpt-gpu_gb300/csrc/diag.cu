@@ -359,6 +359,26 @@ int64_t diag_partial_count(const Grid& g) {
 
 int diag_nred() { return NRED; }
 
+// x-y tiles of the diagnostics grid: ceil(nx/32) * ceil(ny/4).
+int64_t diag_tiles_xy(const Grid& g) { return (int64_t)((g.nx + DX_ - 1) / DX_) * ((g.ny + DY_ - 1) / DY_); }
+
+// Same reduction as launch_diag on a grid of at most max_rows blocks (the z
+// planes folded into each block's loop), for callers that supply a fixed
+// scratch area of max_rows partial rows.  The caller checks
+// diag_tiles_xy(g) <= max_rows.
+cudaError_t launch_diag_bounded(const Grid& g, const ewpt_params& p, const double* y, double* part,
+                                int64_t max_rows, double* dres, cudaStream_t st) {
+    dim3 gr = diag_grid(g);
+    const int64_t xy = (int64_t)gr.x * gr.y;
+    int64_t bz = max_rows / xy;
+    if (bz > (int64_t)gr.z) bz = gr.z;
+    if (bz < 1) bz = 1;
+    gr.z = (unsigned)bz;
+    k_diag_partial<<<gr, dim3(DX_, DY_), 0, st>>>(g, y, diag_coef(p), part);
+    k_diag_final<<<1, 256, 0, st>>>(part, gr.x * gr.y * gr.z, dres);
+    return cudaGetLastError();
+}
+
 void diag_finish_row(const ewpt_params& p, int64_t S, const double* r, double* out) { finish_row(p, S, r, out); }
 
 cudaError_t launch_fields(const Grid& g, const ewpt_params& p, const double* y, int which, double* f,

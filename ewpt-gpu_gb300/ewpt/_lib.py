@@ -68,6 +68,7 @@ def _sig(L):
     L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
     L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_kc_bin_nums.restype = C.c_int64
+    L.ewpt_diagnostics_noalloc.argtypes = [P, C.c_void_p, DP, C.c_void_p]
 
 
 def load():

@@ -153,6 +153,23 @@ int ewpt_spectrum(ewpt_ctx* ctx, int32_t field, int32_t mode, int32_t nbins, dou
  * spec_routines.jl:32-43), -1 on bad input. */
 int64_t ewpt_kc_bin_nums(int32_t cx, int32_t cy, int32_t cz);
 
+/* Snapshot diagnostics (the same 20 columns as ewpt_diagnostics) of a
+ * caller-owned FP64 state, without allocating any device memory.  No
+ * counterpart in the reference: it is for callers that cannot let the
+ * library call cudaMalloc, e.g. a process whose device memory belongs to
+ * another allocator's pool, or a loop that must keep its device footprint
+ * fixed.  `state` is a device pointer to 36*nx*ny*nz doubles in the order
+ * above (packed, array-major); `out` is host memory; work is queued on
+ * `stream` (a cudaStream_t or NULL) and the call waits for it.
+ * Scratch lives in one fixed device array per GPU (about 0.7 MB, held until
+ * the process exits), sized for at most 4096 x-y tiles of 32x4 sites
+ * (ceil(nx/32)*ceil(ny/4) <= 4096, e.g. nx = ny = 512); larger lattices are
+ * rejected with EWPT_ERR_ARG.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Calls share the array and each one overwrites it: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller. */
+int ewpt_diagnostics_noalloc(const ewpt_params* p, const double* state, double out[EWPT_NDIAG], void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -172,9 +172,14 @@ def run_ours(args, ws, rank, local):
     y0 = ewpt.ic.bubbles_tanh(shape, p64.dx, N_BUBBLES, seed=1234 + rank)
     hbm, peak_kind = peaks()
     res = {}
+    from ewpt import autotune
+
+    tiles = {}
     # ---------------------------------------------------------------- FP64
     with ewpt.Lattice(p64) as lat:
         lat.set_state(y0)
+        if not args.no_tune:
+            tiles["fp64"] = autotune.tune(lat)
         barrier(ws)
         with Clocks(local) as ck:
             t = time_steps(lat, args.steps, args.warmup)
@@ -211,6 +216,8 @@ def run_ours(args, ws, rank, local):
         p32.device = local
         with ewpt.Lattice(p32) as lat:
             lat.set_state(y0)
+            if not args.no_tune:
+                tiles["fp32"] = autotune.tune(lat)
             barrier(ws)
             k32 = max(args.steps, 10)
             t = allmax(ws, time_steps(lat, k32, args.warmup))
@@ -241,7 +248,8 @@ def run_ours(args, ws, rank, local):
                                "lambda=0.129, g=0.65, g'=0.35, vev=1, gp2=0.99, gamma=beta=Jex=0",
                    "lattice": [n, n, n], "form": "FP64",
                    "l2": f"inputs larger than L2 (state {36 * S * 8 / 1e9:.2f} GB per replica)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}",
+                   "tiling": {k: list(v) for k, v in tiles.items()}},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                      "traffic": None, "peak_kind": peak_kind, "kernel": "k_stage_fp64 (4 launches/step)",
                      "algorithmic_bytes_per_site_update": BYTES_FP64,
@@ -353,6 +361,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default 32x4 tiling")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -109,7 +109,7 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         if (e == cudaSuccess) e = cudaMalloc(&c->xb, n * 8);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->y, 0, n * 8, c->st);
     } else {
-        float** bufs[] = {&c->y32.hi, &c->y32.lo, &c->w32.k1, &c->w32.k2, &c->w32.k3, &c->w32.xa, &c->w32.xb};
+        float** bufs[] = {&c->y32.hi, &c->y32.lo, &c->w32.kacc, &c->w32.xa, &c->w32.xb};
         e = cudaSuccess;
         for (float** b : bufs)
             if (e == cudaSuccess) e = cudaMalloc(b, n * 4);
@@ -137,9 +137,7 @@ int ewpt_destroy(ewpt_ctx* c) {
     cudaFree(c->xb);
     cudaFree(c->y32.hi);
     cudaFree(c->y32.lo);
-    cudaFree(c->w32.k1);
-    cudaFree(c->w32.k2);
-    cudaFree(c->w32.k3);
+    cudaFree(c->w32.kacc);
     cudaFree(c->w32.xa);
     cudaFree(c->w32.xb);
     cudaFree(c->scratch64);
@@ -235,9 +233,9 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         const double G = expl ? gam : damp_of(c->p, it);
         cudaError_t e;
         if (c->p.precision == EWPT_FP64)
-            e = launch_step_fp64(c->g, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+            e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
         else
-            e = launch_step_fp32(c->g, c->y32, c->w32, c->p, J, G, c->st);
+            e = launch_step_fp32(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st);
         int rc = ewpt_cuda_check(c, e, "step launch");
         if (rc) return rc;
         c->it = it;
@@ -252,6 +250,24 @@ int ewpt_step_explicit(ewpt_ctx* c, int32_t nsteps, double Jex, double gamma) {
 }
 
 int64_t ewpt_iteration(const ewpt_ctx* c) { return c ? c->it : -1; }
+
+int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (reg < 0 || reg > 2) return ewpt_fail(c, EWPT_ERR_ARG, "register variant %d unknown (0..2)", reg);
+    if (bx < 1 || by < 1 || bx * by > tiling_max_threads(reg) || (bx * by) % 32 != 0)
+        return ewpt_fail(c, EWPT_ERR_ARG, "tile %dx%d: need whole warps and at most %d threads for variant %d", bx, by,
+                         tiling_max_threads(reg), reg);
+    c->tile = Tiling{bx, by, reg};
+    return EWPT_OK;
+}
+
+int ewpt_get_tiling(const ewpt_ctx* c, int32_t* bx, int32_t* by, int32_t* reg) {
+    if (!c || !bx || !by || !reg) return ewpt_fail(nullptr, EWPT_ERR_ARG, "NULL argument");
+    *bx = c->tile.bx;
+    *by = c->tile.by;
+    *reg = c->tile.reg;
+    return EWPT_OK;
+}
 
 int ewpt_sync(ewpt_ctx* c) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");

@@ -10,14 +10,15 @@ struct ewpt_ctx {
     Grid g{};
     cudaStream_t st = nullptr;
     int64_t it = 0;  // RK4 iterations done (the reference's loop counter)
+    Tiling tile = kDefaultTiling;  // stage-kernel launch shape
     // FP64 form: state y, accumulator yn, stage inputs xa/xb, each [36][S]
     double* y = nullptr;
     double* yn = nullptr;
     double* xa = nullptr;
     double* xb = nullptr;
-    // FP32 form: compensated state, stage rates k1..k3, float stage inputs
+    // FP32 form: compensated state, weighted rate sum, float stage inputs
     Fp32State y32{nullptr, nullptr};
-    Fp32Work w32{nullptr, nullptr, nullptr, nullptr, nullptr};
+    Fp32Work w32{nullptr, nullptr, nullptr};
     // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
     double* scratch64 = nullptr;
     // diagnostics / spectra scratch (diag.cu, spectrum.cu)

@@ -83,18 +83,24 @@ struct Fp32State {
     float* lo;  // [36][S]
 };
 struct Fp32Work {
-    float* k1;  // [36][S] stage rates k1..k3
-    float* k2;
-    float* k3;
-    float* xa;  // [36][S] stage inputs (ping-pong)
+    float* kacc;  // [36][S] RK4-weighted sum of the stage rates
+    float* xa;    // [36][S] stage inputs (ping-pong)
     float* xb;
 };
 
 cudaError_t launch_rates_fp64(const Grid& g, const Ptr36& in, const MPtr36& out, const ewpt_params& p,
                               double Jex, double gam, cudaStream_t st);
-cudaError_t launch_step_fp64(const Grid& g, double* y, double* yn, double* xa, double* xb,
+// Launch shape of the stage kernels: (bx, by) threads over x and y, one z
+// plane per grid slice; reg selects the register-budget variant (stage.cu).
+struct Tiling {
+    int bx, by, reg;
+};
+constexpr Tiling kDefaultTiling{32, 4, 0};
+int tiling_max_threads(int reg);
+
+cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
-cudaError_t launch_step_fp32(const Grid& g, Fp32State y, Fp32Work w, const ewpt_params& p, double Jex,
-                             double gam, cudaStream_t st);
+cudaError_t launch_step_fp32(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
+                             double Jex, double gam, cudaStream_t st);
 cudaError_t launch_fp32_split(const Grid& g, const double* src, Fp32State dst, cudaStream_t st);
 cudaError_t launch_fp32_join(const Grid& g, Fp32State src, double* dst, cudaStream_t st);

@@ -1,0 +1,65 @@
+// f32x2.cuh -- packed pair-of-float arithmetic for two lattice sites at once.
+//
+// sm_100-class GPUs issue FADD2/FMUL2/FFMA2: one instruction operates on a
+// pair of floats.  The FP32-form stage kernel gives each thread two
+// x-adjacent sites and runs the ordinary templated physics (physics.cuh) on
+// this pair type, so every flux operation is one packed instruction for two
+// sites.  A product is kept unevaluated (Prod) until it meets an addition, so
+// `a * b + c` becomes a single FFMA2 as the scalar compiler would contract it.
+#pragma once
+#include <cuda_runtime.h>
+
+struct f2;
+struct Prod;
+
+struct f2 {
+    float2 v;
+    __device__ __forceinline__ f2() {}
+    __device__ __forceinline__ f2(float2 x) : v(x) {}
+    __device__ __forceinline__ explicit f2(float s) : v(make_float2(s, s)) {}
+    __device__ __forceinline__ explicit f2(double s) : v(make_float2((float)s, (float)s)) {}
+    __device__ __forceinline__ explicit f2(int s) : v(make_float2((float)s, (float)s)) {}
+    __device__ __forceinline__ f2(const Prod& p);
+    __device__ __forceinline__ f2& operator+=(const f2& b);
+    __device__ __forceinline__ f2& operator-=(const f2& b);
+    __device__ __forceinline__ f2& operator+=(const Prod& b);
+    __device__ __forceinline__ f2& operator-=(const Prod& b);
+};
+
+struct Prod {
+    float2 a, b;
+    __device__ __forceinline__ float2 eval() const { return __fmul2_rn(a, b); }
+};
+
+__device__ __forceinline__ float2 neg2(float2 x) { return make_float2(-x.x, -x.y); }
+
+__device__ __forceinline__ f2::f2(const Prod& p) : v(p.eval()) {}
+
+// products
+__device__ __forceinline__ Prod operator*(const f2& a, const f2& b) { return Prod{a.v, b.v}; }
+__device__ __forceinline__ Prod operator*(const Prod& a, const f2& b) { return Prod{a.eval(), b.v}; }
+__device__ __forceinline__ Prod operator*(const f2& a, const Prod& b) { return Prod{a.v, b.eval()}; }
+__device__ __forceinline__ Prod operator*(const Prod& a, const Prod& b) { return Prod{a.eval(), b.eval()}; }
+__device__ __forceinline__ Prod operator-(const Prod& p) { return Prod{neg2(p.a), p.b}; }
+
+// sums
+__device__ __forceinline__ f2 operator+(const f2& a, const f2& b) { return __fadd2_rn(a.v, b.v); }
+__device__ __forceinline__ f2 operator-(const f2& a, const f2& b) { return __fadd2_rn(a.v, neg2(b.v)); }
+__device__ __forceinline__ f2 operator-(const f2& a) { return neg2(a.v); }
+__device__ __forceinline__ f2 operator+(const f2& x, const Prod& p) { return __ffma2_rn(p.a, p.b, x.v); }
+__device__ __forceinline__ f2 operator+(const Prod& p, const f2& x) { return __ffma2_rn(p.a, p.b, x.v); }
+__device__ __forceinline__ f2 operator+(const Prod& p, const Prod& q) { return __ffma2_rn(q.a, q.b, p.eval()); }
+__device__ __forceinline__ f2 operator-(const f2& x, const Prod& p) { return __ffma2_rn(neg2(p.a), p.b, x.v); }
+__device__ __forceinline__ f2 operator-(const Prod& p, const f2& x) { return __ffma2_rn(p.a, p.b, neg2(x.v)); }
+__device__ __forceinline__ f2 operator-(const Prod& p, const Prod& q) { return __ffma2_rn(neg2(q.a), q.b, p.eval()); }
+
+// one division per site in the physics (1/|Phi|^2): two scalar divides
+__device__ __forceinline__ f2 operator/(const f2& a, const f2& b) {
+    return make_float2(a.v.x / b.v.x, a.v.y / b.v.y);
+}
+__device__ __forceinline__ f2 operator/(const f2& a, const Prod& b) { return a / f2(b); }
+
+__device__ __forceinline__ f2& f2::operator+=(const f2& b) { return *this = *this + b; }
+__device__ __forceinline__ f2& f2::operator-=(const f2& b) { return *this = *this - b; }
+__device__ __forceinline__ f2& f2::operator+=(const Prod& b) { return *this = *this + b; }
+__device__ __forceinline__ f2& f2::operator-=(const Prod& b) { return *this = *this - b; }

@@ -14,14 +14,26 @@
 //   stage 3: k = f(X3);  yn = yn + k dt/3;  X4 = y + k dt
 //   stage 4: k = f(X4);  y  = yn + k dt/6
 // FP32 form (FP32 stencils and fluxes, compensated float hi/lo state):
-//   stage s < 4: k_s = f(X_s) stored as float, X_{s+1} = y_hi + c_s k_s
-//   stage 4:     (y_hi, y_lo) += dt/6 (k1 + 2 k2 + 2 k3 + k4), in place
+//   stage 1:     kacc = k1;           X2 = y_hi + k1 dt/2
+//   stage 2, 3:  kacc += 2 k_s;       X3 = y_hi + k2 dt/2,  X4 = y_hi + k3 dt
+//   stage 4:     (y_hi, y_lo) += dt/6 (kacc + k4), compensated, in place
 // (X_1 is y_hi itself).  Bytes per site-update: FP64 4608, FP32 2736.
 #include "ewpt_internal.cuh"
 
 namespace {
 
-constexpr int BX = 32, BY = 4;
+// Register-budget variants of the stage kernels (launch bounds, blocks of at
+// most 128 threads): 0 = registers at the compiler's choice (up to 255);
+// 1 = at most 128 registers (4 blocks per SM); 2 = at most 168 registers (3
+// blocks per SM).  The block shape (bx, by) is a launch parameter.
+template <int REG>
+struct RegBudget;
+template <>
+struct RegBudget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
+template <>
+struct RegBudget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
+template <>
+struct RegBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
 
 // Stage input read from global memory through the read-only path.
 template <typename TL, typename T>
@@ -77,8 +89,8 @@ struct GlobalAcc {
 
 template <typename TL, typename T>
 __device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc, GlobalAcc<TL, T>& A) {
-    const int i = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return false;
     A.c = i + g.nx * (j + g.ny * k);
@@ -97,7 +109,7 @@ struct RatesSink {
 };
 
 template <bool BETA>
-__global__ void __launch_bounds__(BX* BY) k_rates_fp64(Grid g, const __grid_constant__ Ptr36 X,
+__global__ void __launch_bounds__(256) k_rates_fp64(Grid g, const __grid_constant__ Ptr36 X,
                                                        const __grid_constant__ MPtr36 R, PhysCoef<double> pc,
                                                        StencilCoef<double> sc) {
     GlobalAcc<double, double> A{X};
@@ -123,16 +135,18 @@ struct Fp64Sink {
             yn[q] = fma(r, w, ya);
             xn[q] = fma(r, h, ya);
         } else if (STAGE < 4) {
-            yn[q] = fma(r, w, yn[q]);
+            // yn[q] is read and then written by this thread only: the
+            // read-only path lets these loads issue ahead of earlier stores
+            yn[q] = fma(r, w, __ldg(yn + q));
             xn[q] = fma(r, h, __ldg(y + q));
         } else {
-            acc_out[q] = fma(r, w, yn[q]);
+            acc_out[q] = fma(r, w, __ldg(yn + q));
         }
     }
 };
 
-template <int STAGE, bool BETA>
-__global__ void __launch_bounds__(BX* BY) k_stage_fp64(Grid g, const __grid_constant__ Ptr36 X,
+template <int STAGE, bool BETA, int REG>
+__global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks) k_stage_fp64(Grid g, const __grid_constant__ Ptr36 X,
                                                        const double* __restrict__ y, double* yn,
                                                        double* __restrict__ xn, double* acc_out,
                                                        PhysCoef<double> pc, StencilCoef<double> sc, double w,
@@ -157,9 +171,7 @@ __device__ __forceinline__ void acc2(float& hi, float& lo, float p) {
 struct Fp32Bufs {
     float* yhi;  // [36][S] state, high part (also the stage-1 stencil input)
     float* ylo;  // [36][S] state, low part
-    float* k1;   // [36][S] stage rates
-    float* k2;
-    float* k3;
+    float* kacc; // [36][S] RK4-weighted rate sum: k1, then k1 + 2 k2, then k1 + 2 k2 + 2 k3
 };
 
 template <int STAGE>
@@ -172,14 +184,16 @@ struct Fp32Sink {
     __device__ __forceinline__ void operator()(int a, float r) const {
         const int64_t q = a * S + A.c;
         if (STAGE == 1) {
-            b.k1[q] = r;
+            b.kacc[q] = r;
             xn[q] = A.v(a) + h * r;  // X1 == y_hi
         } else if (STAGE < 4) {
-            (STAGE == 2 ? b.k2 : b.k3)[q] = r;
+            // kacc[q], yhi[q], ylo[q] are read and then written by this thread
+            // only: the read-only path lets the loads issue ahead of stores
+            b.kacc[q] = __ldg(b.kacc + q) + 2.f * r;
             xn[q] = __ldg(b.yhi + q) + h * r;
         } else {
-            const float s = (b.k1[q] + r) + 2.f * (b.k2[q] + b.k3[q]);
-            float hi = b.yhi[q], lo = b.ylo[q];
+            const float s = __ldg(b.kacc + q) + r;
+            float hi = __ldg(b.yhi + q), lo = __ldg(b.ylo + q);
             acc2(hi, lo, w6 * s);
             b.yhi[q] = hi;
             b.ylo[q] = lo;
@@ -187,8 +201,8 @@ struct Fp32Sink {
     }
 };
 
-template <int STAGE, bool BETA>
-__global__ void __launch_bounds__(BX* BY) k_stage_fp32(Grid g, const __grid_constant__ Ptr36 X, Fp32Bufs b,
+template <int STAGE, bool BETA, int REG>
+__global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks) k_stage_fp32(Grid g, const __grid_constant__ Ptr36 X, Fp32Bufs b,
                                                        float* __restrict__ xn, PhysCoef<float> pc,
                                                        StencilCoef<float> sc, float h, float w6) {
     GlobalAcc<float, float> A{X};
@@ -212,7 +226,9 @@ __global__ void k_join(int64_t n, const float* __restrict__ hi, const float* __r
         dst[q] = (double)hi[q] + (double)lo[q];
 }
 
-inline dim3 grid_of(const Grid& g) { return dim3((g.nx + BX - 1) / BX, (g.ny + BY - 1) / BY, g.nz); }
+inline dim3 grid_of(const Grid& g, const Tiling& t) {
+    return dim3((g.nx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz);
+}
 
 Ptr36 pack(const void* base, int64_t S, size_t elem) {
     Ptr36 P;
@@ -222,61 +238,84 @@ Ptr36 pack(const void* base, int64_t S, size_t elem) {
 
 }  // namespace
 
+int tiling_max_threads(int reg) { return reg >= 0 && reg <= 2 ? 128 : 0; }
+
 cudaError_t launch_rates_fp64(const Grid& g, const Ptr36& in, const MPtr36& out, const ewpt_params& p,
                               double Jex, double gam, cudaStream_t st) {
     const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
     const StencilCoef<double> sc = make_stencil<double>(p.dx);
     const bool beta = p.beta_w != 0.0 || p.beta_y != 0.0;
     if (beta)
-        k_rates_fp64<true><<<grid_of(g), dim3(BX, BY), 0, st>>>(g, in, out, pc, sc);
+        k_rates_fp64<true><<<grid_of(g, kDefaultTiling), dim3(32, 4), 0, st>>>(g, in, out, pc, sc);
     else
-        k_rates_fp64<false><<<grid_of(g), dim3(BX, BY), 0, st>>>(g, in, out, pc, sc);
+        k_rates_fp64<false><<<grid_of(g, kDefaultTiling), dim3(32, 4), 0, st>>>(g, in, out, pc, sc);
     return cudaGetLastError();
 }
 
-template <bool BETA>
-static void step_fp64(const Grid& g, double* y, double* yn, double* xa, double* xb, const PhysCoef<double>& pc,
-                      const StencilCoef<double>& sc, double dt, cudaStream_t st) {
-    const dim3 gr = grid_of(g), bl(BX, BY);
-    k_stage_fp64<1, BETA><<<gr, bl, 0, st>>>(g, pack(y, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 6., dt / 2.);
-    k_stage_fp64<2, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.);
-    k_stage_fp64<3, BETA><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 3., dt);
-    k_stage_fp64<4, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
+template <bool BETA, int REG>
+static void step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
+                      const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+    const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
+    k_stage_fp64<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack(y, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 6., dt / 2.);
+    k_stage_fp64<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.);
+    k_stage_fp64<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 3., dt);
+    k_stage_fp64<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
 }
 
-cudaError_t launch_step_fp64(const Grid& g, double* y, double* yn, double* xa, double* xb, const ewpt_params& p,
-                             double Jex, double gam, cudaStream_t st) {
+template <bool BETA>
+static void step_fp64_r(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
+                        const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+    if (t.reg == 1)
+        step_fp64<BETA, 1>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+    else if (t.reg == 2)
+        step_fp64<BETA, 2>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+    else
+        step_fp64<BETA, 0>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+}
+
+cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
+                             const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
     const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
     const StencilCoef<double> sc = make_stencil<double>(p.dx);
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_fp64<true>(g, y, yn, xa, xb, pc, sc, p.dt, st);
+        step_fp64_r<true>(g, t, y, yn, xa, xb, pc, sc, p.dt, st);
     else
-        step_fp64<false>(g, y, yn, xa, xb, pc, sc, p.dt, st);
+        step_fp64_r<false>(g, t, y, yn, xa, xb, pc, sc, p.dt, st);
     return cudaGetLastError();
 }
 
-// FP32 form.  yn.hi/yn.lo/xb are reused as the k1/k2/k3 stores; xa and
-// the second half of the k buffers hold the two stage-input ping-pong arrays.
-template <bool BETA>
-static void step_fp32(const Grid& g, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
+// FP32 form: stage inputs ping-pong between xa and xb.
+template <bool BETA, int REG>
+static void step_fp32(const Grid& g, const Tiling& t, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
                       const StencilCoef<float>& sc, double dt, cudaStream_t st) {
-    const dim3 gr = grid_of(g), bl(BX, BY);
+    const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
     const float h2 = (float)(dt / 2.), h1 = (float)dt, w6 = (float)(dt / 6.);
-    k_stage_fp32<1, BETA><<<gr, bl, 0, st>>>(g, pack(b.yhi, g.S, 4), b, xa, pc, sc, h2, w6);
-    k_stage_fp32<2, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, xb, pc, sc, h2, w6);
-    k_stage_fp32<3, BETA><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 4), b, xa, pc, sc, h1, w6);
-    k_stage_fp32<4, BETA><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, nullptr, pc, sc, 0.f, w6);
+    k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack(b.yhi, g.S, 4), b, xa, pc, sc, h2, w6);
+    k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, xb, pc, sc, h2, w6);
+    k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 4), b, xa, pc, sc, h1, w6);
+    k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, nullptr, pc, sc, 0.f, w6);
 }
 
-cudaError_t launch_step_fp32(const Grid& g, Fp32State y, Fp32Work w, const ewpt_params& p, double Jex, double gam,
-                             cudaStream_t st) {
+template <bool BETA>
+static void step_fp32_r(const Grid& g, const Tiling& t, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
+                        const StencilCoef<float>& sc, double dt, cudaStream_t st) {
+    if (t.reg == 1)
+        step_fp32<BETA, 1>(g, t, b, xa, xb, pc, sc, dt, st);
+    else if (t.reg == 2)
+        step_fp32<BETA, 2>(g, t, b, xa, xb, pc, sc, dt, st);
+    else
+        step_fp32<BETA, 0>(g, t, b, xa, xb, pc, sc, dt, st);
+}
+
+cudaError_t launch_step_fp32(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
+                             double Jex, double gam, cudaStream_t st) {
     const PhysCoef<float> pc = make_phys<float>(p, Jex, gam);
     const StencilCoef<float> sc = make_stencil<float>(p.dx);
-    Fp32Bufs b{y.hi, y.lo, w.k1, w.k2, w.k3};
+    Fp32Bufs b{y.hi, y.lo, w.kacc};
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_fp32<true>(g, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_fp32_r<true>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     else
-        step_fp32<false>(g, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_fp32_r<false>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     return cudaGetLastError();
 }
 

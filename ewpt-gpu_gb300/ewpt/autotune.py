@@ -1,0 +1,103 @@
+"""Tile-shape autotuner for the stage kernels.
+
+Times every candidate launch shape (block bx x by over x-y, register-budget
+variant reg; see ewpt_set_tiling in include/ewpt.h) on a scratch lattice of
+the same size and precision, with CUDA events on the library's stream, and
+caches the fastest per (lattice shape, precision, beta on/off, GPU name) in a
+JSON file (default ~/.cache/ewpt/autotune.json, or $EWPT_AUTOTUNE_CACHE).
+The result does not change any number the kernels compute, only their speed.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+from . import _lib, ic
+from .lattice import Lattice
+from .params import Params
+
+CANDIDATES = [(32, 4, 0), (64, 2, 0), (32, 2, 0), (16, 8, 0), (128, 1, 0),
+              (32, 4, 1), (64, 2, 1), (32, 2, 1), (16, 8, 1),
+              (32, 4, 2), (64, 2, 2), (32, 2, 2), (16, 8, 2)]
+
+
+def cache_path() -> str:
+    return os.environ.get("EWPT_AUTOTUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "ewpt",
+                                                               "autotune.json"))
+
+
+def _key(p: Params) -> str:
+    import torch
+
+    nx, ny, nz = p.dims
+    beta = int(p.beta_w != 0.0 or p.beta_y != 0.0)
+    return f"{nx}x{ny}x{nz}:p{int(p.precision)}:b{beta}:{torch.cuda.get_device_name(p.device)}"
+
+
+def _load_cache() -> dict:
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _save_cache(d: dict):
+    path = cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
+def time_tiling(lat: Lattice, tile, steps: int = 2) -> float:
+    """Seconds per RK4 step with the given tiling (CUDA events on the lattice's stream)."""
+    import torch
+
+    lat.set_tiling(*tile)
+    st = torch.cuda.ExternalStream(lat.stream)
+    lat.step(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    lat.step(steps)
+    e1.record(st)
+    lat.sync()
+    return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def sweep(p: Params, steps: int = 2, candidates=None) -> list:
+    """(tiling, seconds per step) for every candidate on a scratch lattice."""
+    candidates = candidates or CANDIDATES
+    res = []
+    with Lattice(p) as lat:
+        lat.set_state(ic.bubbles_tanh(p.dims, p.dx, 4, seed=0))
+        for t in candidates:
+            try:
+                res.append((t, time_tiling(lat, t, steps)))
+            except _lib.EwptError:
+                continue
+    return res
+
+
+def best_tiling(p: Params, steps: int = 2, use_cache: bool = True) -> tuple:
+    key = _key(p)
+    cache = _load_cache() if use_cache else {}
+    if key in cache:
+        return tuple(cache[key]["tile"])
+    res = sweep(p, steps)
+    tile, t = min(res, key=lambda r: r[1])
+    cache[key] = {"tile": list(tile), "s_per_step": t, "sweep": [[list(a), b] for a, b in res]}
+    if use_cache:
+        _save_cache(cache)
+    return tile
+
+
+def tune(lat: Lattice, steps: int = 2) -> tuple:
+    """Apply the cached (or freshly measured) best tiling to `lat`."""
+    tile = best_tiling(lat.params, steps)
+    lat.set_tiling(*tile)
+    return tile

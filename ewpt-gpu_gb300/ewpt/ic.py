@@ -116,3 +116,234 @@ def bubbles_tanh(shape, dx, nbub, lam=0.129, vev=1.0, seed=0, radius=None, width
         for a in range(4):
             y[a] += dirs[b, a] * prof
     return y
+
+
+# ----------------------------------------------------------------- thermal
+def _kgrid(shape, dx):
+    """Per-axis lattice wave numbers theta = 2 pi n / N (n the wrapped FFT index)."""
+    return [2.0 * np.pi * np.fft.fftfreq(n) for n in shape]
+
+
+def _deriv_symbol(theta, dx):
+    """Fourier symbol s(theta) of the 6th-order first derivative
+    (diff_scheme.jl:157-233): d/dx e^{i k x} = i s e^{i k x}."""
+    return (90.0 * np.sin(theta) - 18.0 * np.sin(2 * theta) + 2.0 * np.sin(3 * theta)) / (60.0 * dx)
+
+
+def _real_field(rng, amp, shape):
+    """real(bfft(amp * (r + i r')))/1 with r, r' ~ N(0, sqrt 2) per mode, the
+    construction of main_rk4.jl:5352-5600 (unnormalised backward FFT)."""
+    z = amp * (rng.normal(0.0, math.sqrt(2.0), amp.shape) + 1j * rng.normal(0.0, math.sqrt(2.0), amp.shape))
+    return np.real(np.fft.ifftn(z) * z.size)
+
+
+def _grad(f, sym):
+    F = np.fft.fftn(f)
+    return [np.real(np.fft.ifftn(1j * s * F)) for s in sym]
+
+
+def _div(fx, fy, fz, sym):
+    out = 0
+    for f, s in zip((fx, fy, fz), sym):
+        out = out + np.fft.fftn(f) * (1j * s)
+    return np.real(np.fft.ifftn(out))
+
+
+def thermal(shape, dx, T=1.5, lam=0.129, gw=0.65, gy=0.35, vev=1.0, seed=0, mH=None, mW=None,
+            gauss_iters=20, with_momenta=True):
+    """Thermal initial condition (BASELINE precision configuration).
+
+    Gaussian random Higgs and gauge modes with Bose-Einstein occupation
+    n(w) = 1/(exp(w/T) - 1): Higgs w^2 = k^2 + mH^2 (mH = sqrt(2 lambda) vev),
+    gauge w^2 = k^2 + mW^2 (mW = g vev/2) with two transverse polarisations
+    (thermal_initializer_phi!/gauge!, main_rk4.jl:5029-5152: field amplitude
+    sqrt(n/(w V)), real part of the unnormalised backward FFT), with
+    k^2 = sum_i 2(1 - cos(k_i dx))/dx^2.  Momenta get amplitude sqrt(n w / V)
+    (the reference leaves them zero) and the electric fields are then
+    projected onto the discrete Gauss law d_i E^a_i = rho^a,
+    d_i E_i(Y) = rho_Y, with the 6th-order derivative's Fourier symbol and a
+    fixed-point iteration over the E-dependent SU(2) charge.  Gamma_a =
+    d_i W^a_i and Sigma = d_i Y_i.  The zero mode of rho (total charge)
+    cannot be projected out on a periodic box and remains."""
+    rng = np.random.default_rng(seed)
+    shape = tuple(shape)
+    nx, ny, nz = shape
+    mH = math.sqrt(2.0 * lam) * vev if mH is None else mH
+    mW = gw * vev / 2.0 if mW is None else mW
+    # numpy arrays in (z, y, x) order so that ravel() is the Julia layout
+    th = _kgrid((nz, ny, nx), dx)
+    TZ, TY, TX = np.meshgrid(*th, indexing="ij")
+    k2 = 2.0 * ((1 - np.cos(TX)) + (1 - np.cos(TY)) + (1 - np.cos(TZ))) / dx ** 2
+    vol = nx * ny * nz * dx ** 3
+
+    def occ(w):
+        with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+            n = 1.0 / np.expm1(w / T)
+        return np.where(w > 0, n, 0.0)
+
+    wH = np.sqrt(k2 + mH ** 2)
+    wW = np.sqrt(k2 + mW ** 2)
+    nH, nW = occ(wH), occ(wW)
+    aH = np.sqrt(nH / (wH * vol))
+    pH = np.sqrt(nH * wH / vol)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        aW = np.where(wW > 0, np.sqrt(nW / (wW * vol)), 0.0)
+        pW = np.sqrt(nW * wW / vol)
+    zero = (k2 == 0)
+    aW[zero] = 0.0
+    pW[zero] = 0.0
+    # transverse polarisations from the lattice momentum (2 sin(theta/2)/dx)
+    kv = [2.0 * np.sin(0.5 * t) / dx for t in (TX, TY, TZ)]
+
+    def transverse(amp):
+        r = [rng.normal(0.0, math.sqrt(2.0), amp.shape) for _ in range(3)]
+        e1 = [r[1] * kv[2] - r[2] * kv[1], r[2] * kv[0] - r[0] * kv[2], r[0] * kv[1] - r[1] * kv[0]]
+        n1 = np.sqrt(sum(c * c for c in e1))
+        n1[n1 == 0] = 1.0
+        e1 = [c / n1 for c in e1]
+        e2 = [e1[1] * kv[2] - e1[2] * kv[1], e1[2] * kv[0] - e1[0] * kv[2], e1[0] * kv[1] - e1[1] * kv[0]]
+        n2 = np.sqrt(sum(c * c for c in e2))
+        n2[n2 == 0] = 1.0
+        e2 = [c / n2 for c in e2]
+        xs = [rng.normal(0.0, math.sqrt(2.0), amp.shape) + 1j * rng.normal(0.0, math.sqrt(2.0), amp.shape)
+              for _ in range(2)]
+        comps = []
+        for i in range(3):
+            z = amp * (e1[i] * xs[0] + e2[i] * xs[1])
+            comps.append(np.real(np.fft.ifftn(z) * z.size))
+        return comps
+
+    S = nx * ny * nz
+    y = np.zeros((36, S))
+    for a in range(4):
+        y[a] = _real_field(rng, aH, (nz, ny, nx)).ravel()
+        if with_momenta:
+            y[20 + a] = _real_field(rng, pH, (nz, ny, nx)).ravel()
+    for a in range(3):
+        W = transverse(aW)
+        for i in range(3):
+            y[4 + 3 * a + i] = W[i].ravel()
+        if with_momenta:
+            E = transverse(pW)
+            for i in range(3):
+                y[24 + 3 * a + i] = E[i].ravel()
+    aY = np.sqrt(np.where(k2 > 0, occ(np.sqrt(k2)) / np.where(k2 > 0, np.sqrt(k2) * vol, 1.0), 0.0))
+    pY = np.sqrt(np.where(k2 > 0, occ(np.sqrt(k2)) * np.sqrt(k2) / vol, 0.0))
+    Yc = transverse(aY)
+    for i in range(3):
+        y[13 + i] = Yc[i].ravel()
+    if with_momenta:
+        Ec = transverse(pY)
+        for i in range(3):
+            y[33 + i] = Ec[i].ravel()
+    sym = [_deriv_symbol(t, dx) for t in (TX, TY, TZ)]
+    # auxiliaries consistent with the gauge fields
+    for a in range(3):
+        y[16 + a] = _div(*[y[4 + 3 * a + i].reshape(nz, ny, nx) for i in range(3)], sym).ravel()
+    y[19] = _div(*[y[13 + i].reshape(nz, ny, nx) for i in range(3)], sym).ravel()
+    if with_momenta:
+        gauss_project(y, shape, dx, gw, gy, iters=gauss_iters, sym=sym)
+    return y
+
+
+def gauss_charges(y, gw, gy):
+    """SU(2) and U(1) charge densities of main_rk4.jl:603-655 (the terms
+    multiplying gp2 in k_Gamma_a and k_Sigma)."""
+    p1, p2, p3, p4 = y[0], y[1], y[2], y[3]
+    t1, t2, t3, t4 = y[20], y[21], y[22], y[23]
+    W = [[y[4 + 3 * a + i] for i in range(3)] for a in range(3)]
+    E = [[y[24 + 3 * a + i] for i in range(3)] for a in range(3)]
+    hig = [p1 * t4 - p4 * t1 + p3 * t2 - p2 * t3, p3 * t1 - p1 * t3 + p4 * t2 - p2 * t4,
+           p1 * t2 - p2 * t1 + p4 * t3 - p3 * t4]
+    rho = []
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        q = -sum(W[b][i] * E[c][i] - W[c][i] * E[b][i] for i in range(3))
+        rho.append(gw * q + gw * hig[a])
+    rhoY = gy * (p1 * t2 - p2 * t1 + p3 * t4 - p4 * t3)
+    return rho, rhoY
+
+
+# phi^T M pi of the Higgs charges of k_Gamma_1..3 and k_Sigma (main_rk4.jl:603-655)
+_CHARGE_PAIRS = [[(0, 3), (2, 1)], [(2, 0), (3, 1)], [(0, 1), (3, 2)], [(0, 1), (2, 3)]]
+
+
+def _charge_matrix(a):
+    M = np.zeros((4, 4))
+    for i, j in _CHARGE_PAIRS[a]:
+        M[i, j] = 1.0
+        M[j, i] = -1.0
+    return M
+
+
+def _null_patterns(shape):
+    """Staggered patterns (-1)^(e.x), e in {0,1}^3 (only e_i = 1 on even axes):
+    the modes that the central-difference divergence cannot produce."""
+    nx, ny, nz = shape
+    i = np.arange(nx)
+    j = np.arange(ny)
+    k = np.arange(nz)
+    pats = []
+    for ez in (0, 1) if nz % 2 == 0 else (0,):
+        for ey in (0, 1) if ny % 2 == 0 else (0,):
+            for ex in (0, 1) if nx % 2 == 0 else (0,):
+                P = ((-1.0) ** (ez * k))[:, None, None] * ((-1.0) ** (ey * j))[None, :, None] * \
+                    ((-1.0) ** (ex * i))[None, None, :]
+                pats.append(P.ravel())
+    return pats
+
+
+def neutralize_charges(y, gw, gy, shape):
+    """Shift the Higgs momenta along the four charge generators so that the
+    charges have no component in the null modes of the central-difference
+    divergence (the zero mode and the Nyquist corners, where d_i E_i is 0
+    whatever E is): Gauss's law can only hold for such a charge density."""
+    rho, rhoY = gauss_charges(y, gw, gy)
+    dens = list(rho) + [rhoY]
+    coup = [gw, gw, gw, gy]
+    pats = _null_patterns(shape)
+    phi = y[0:4]
+    Ms = [_charge_matrix(a) for a in range(4)]
+    MT_phi = [M.T @ phi for M in Ms]
+    # unknowns alpha[b, P]: pi += alpha[b,P] * P(x) * M_b^T phi
+    n = 4 * len(pats)
+    A = np.zeros((n, n))
+    Q = np.zeros(n)
+    for a in range(4):
+        for pi_, P in enumerate(pats):
+            r = a * len(pats) + pi_
+            Q[r] = np.sum(P * dens[a])
+            for b in range(4):
+                g = coup[a] * np.sum(phi * (Ms[a] @ MT_phi[b]), axis=0)  # per-site phi^T M_a M_b^T phi
+                for pj, P2 in enumerate(pats):
+                    A[r, b * len(pats) + pj] = np.sum(P * P2 * g)
+    alpha = np.linalg.lstsq(A, -Q, rcond=None)[0]
+    for b in range(4):
+        for pj, P2 in enumerate(pats):
+            y[20:24] += alpha[b * len(pats) + pj] * P2 * MT_phi[b]
+    return y
+
+
+def gauss_project(y, shape, dx, gw, gy, iters=12, sym=None):
+    """Project the electric fields onto d_i E_i = rho (in place), iterating
+    over the E-dependent part of the SU(2) charge; each iteration first
+    neutralises the total charges (neutralize_charges)."""
+    nx, ny, nz = shape
+    if sym is None:
+        th = _kgrid((nz, ny, nx), dx)
+        TZ, TY, TX = np.meshgrid(*th, indexing="ij")
+        sym = [_deriv_symbol(t, dx) for t in (TX, TY, TZ)]
+    s2 = sym[0] ** 2 + sym[1] ** 2 + sym[2] ** 2
+    ok = s2 > 1e-12 * s2.max()
+    for _ in range(iters):
+        neutralize_charges(y, gw, gy, shape)
+        rho, rhoY = gauss_charges(y, gw, gy)
+        groups = [(24 + 3 * a, rho[a]) for a in range(3)] + [(33, rhoY)]
+        for base, r in groups:
+            Ex, Ey, Ez = (y[base + i].reshape(nz, ny, nx) for i in range(3))
+            F = [np.fft.fftn(Ex), np.fft.fftn(Ey), np.fft.fftn(Ez)]
+            res = 1j * (sym[0] * F[0] + sym[1] * F[1] + sym[2] * F[2]) - np.fft.fftn(r.reshape(nz, ny, nx))
+            chi = np.where(ok, res / np.where(ok, -s2, 1.0), 0.0)
+            for i in range(3):
+                y[base + i] = np.real(np.fft.ifftn(F[i] - 1j * sym[i] * chi)).ravel()
+    return y

@@ -101,6 +101,12 @@ int ewpt_step(ewpt_ctx* ctx, int32_t nsteps);
 int ewpt_step_explicit(ewpt_ctx* ctx, int32_t nsteps, double Jex, double gamma);
 /* Iterations done so far (the `it` of the reference loop). */
 int64_t ewpt_iteration(const ewpt_ctx* ctx);
+/* Launch shape of the stage kernels: blocks of bx*by threads over x and y
+ * (whole warps, at most 128 threads), reg = register-budget variant (0:
+ * registers at the compiler's choice; 1: <= 128 registers; 2: <= 168).  Results do not depend on it; ewpt/autotune.py picks it per
+ * lattice size and precision.  Default 32x4, variant 0. */
+int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg);
+int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg);
 /* Wait for all work queued on the context. */
 int ewpt_sync(ewpt_ctx* ctx);
 /* The context's cudaStream_t, as an opaque pointer. */

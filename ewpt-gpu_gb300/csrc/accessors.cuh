@@ -1,0 +1,176 @@
+// accessors.cuh -- neighbour access for the stage kernels.
+//
+// An accessor serves site_rates (physics.cuh) the values, 6th-order
+// gradients and Laplacians of the 36 stage-input arrays at its site, reading
+// global memory through the read-only path with the periodic wrap folded
+// into the neighbour offsets.  The source of the 36 array pointers is a
+// policy: SrcPtr36 (one pointer per array, kernel parameter) for a single
+// lattice, SrcBase (base + a*S) for members of a batched ensemble.
+#pragma once
+#include "ewpt_internal.cuh"
+#include "f32x2.cuh"
+
+template <typename TL>
+struct SrcPtr36 {
+    const Ptr36& P;
+    __device__ __forceinline__ const TL* arr(int a) const { return reinterpret_cast<const TL*>(P.p[a]); }
+};
+
+template <typename TL>
+struct SrcBase {
+    const TL* base;
+    int64_t S;
+    __device__ __forceinline__ const TL* arr(int a) const { return base + a * S; }
+};
+
+// One site per thread; TL = stored type, T = arithmetic type.
+template <typename TL, typename T, class Src>
+struct SiteAcc {
+    Src src;
+    int c;
+    int ox[6], oy[6], oz[6];
+    StencilCoef<T> s;
+
+    __device__ __forceinline__ T ld(int a, int off) const { return (T)__ldg(src.arr(a) + (c + off)); }
+    __device__ __forceinline__ T v(int a) const { return ld(a, 0); }
+    __device__ __forceinline__ T d1(int a, const int* o) const {
+        return s.a1 * (ld(a, o[0]) - ld(a, o[3])) + s.a2 * (ld(a, o[1]) - ld(a, o[4])) +
+               s.a3 * (ld(a, o[2]) - ld(a, o[5]));
+    }
+    __device__ __forceinline__ void grad(int a, T& gx, T& gy, T& gz) const {
+        gx = d1(a, ox);
+        gy = d1(a, oy);
+        gz = d1(a, oz);
+    }
+    __device__ __forceinline__ void grad_lap(int a, T& gx, T& gy, T& gz, T& lap) const {
+        T s1, s2, s3;
+        {
+            const T p1 = ld(a, ox[0]), p2 = ld(a, ox[1]), p3 = ld(a, ox[2]);
+            const T m1 = ld(a, ox[3]), m2 = ld(a, ox[4]), m3 = ld(a, ox[5]);
+            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 = p1 + m1;
+            s2 = p2 + m2;
+            s3 = p3 + m3;
+        }
+        {
+            const T p1 = ld(a, oy[0]), p2 = ld(a, oy[1]), p3 = ld(a, oy[2]);
+            const T m1 = ld(a, oy[3]), m2 = ld(a, oy[4]), m3 = ld(a, oy[5]);
+            gy = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 += p1 + m1;
+            s2 += p2 + m2;
+            s3 += p3 + m3;
+        }
+        {
+            const T p1 = ld(a, oz[0]), p2 = ld(a, oz[1]), p3 = ld(a, oz[2]);
+            const T m1 = ld(a, oz[3]), m2 = ld(a, oz[4]), m3 = ld(a, oz[5]);
+            gz = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 += p1 + m1;
+            s2 += p2 + m2;
+            s3 += p3 + m3;
+        }
+        lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
+    }
+    __device__ __forceinline__ T div3(int a) const { return d1(a, ox) + d1(a + 1, oy) + d1(a + 2, oz); }
+
+    // site (i, j, k) of an nx x ny x nz box
+    __device__ __forceinline__ void place(int i, int j, int k, int nx, int ny, int nz) {
+        c = i + nx * (j + ny * k);
+        axis_offsets(i, nx, 1, ox);
+        axis_offsets(j, ny, nx, oy);
+        axis_offsets(k, nz, nx * ny, oz);
+    }
+};
+
+// Two x-adjacent sites (i0, i0+1), i0 even, packed float pairs.  The x
+// stencil reads the aligned pairs at i0-4, i0-2, i0, i0+2, i0+4 and re-pairs
+// them into the +-1, +-2, +-3 neighbours; y and z neighbours are aligned
+// pairs of the same x columns.  Needs nx even.
+template <class Src>
+struct PairAcc {
+    Src src;
+    int c;      // linear index of site i0 (even)
+    int ox[4];  // float offsets of the x pairs at i0-4, i0-2, i0+2, i0+4 (wrapped)
+    int oy[6], oz[6];
+    StencilCoef<f2> s;
+
+    __device__ __forceinline__ float2 ld(int a, int off) const {
+        return __ldg(reinterpret_cast<const float2*>(src.arr(a) + (c + off)));
+    }
+    __device__ __forceinline__ f2 v(int a) const { return f2(ld(a, 0)); }
+    __device__ __forceinline__ void xpairs(int a, f2& p1, f2& p2, f2& p3, f2& m1, f2& m2, f2& m3) const {
+        const float2 qm2 = ld(a, ox[0]), qm1 = ld(a, ox[1]), q0 = ld(a, 0), qp1 = ld(a, ox[2]), qp2 = ld(a, ox[3]);
+        p1 = f2(make_float2(q0.y, qp1.x));
+        p2 = f2(qp1);
+        p3 = f2(make_float2(qp1.y, qp2.x));
+        m1 = f2(make_float2(qm1.y, q0.x));
+        m2 = f2(qm1);
+        m3 = f2(make_float2(qm2.y, qm1.x));
+    }
+    __device__ __forceinline__ f2 dx(int a) const {
+        f2 p1, p2, p3, m1, m2, m3;
+        xpairs(a, p1, p2, p3, m1, m2, m3);
+        return s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+    }
+    __device__ __forceinline__ f2 d1(int a, const int* o) const {
+        return s.a1 * (f2(ld(a, o[0])) - f2(ld(a, o[3]))) + s.a2 * (f2(ld(a, o[1])) - f2(ld(a, o[4]))) +
+               s.a3 * (f2(ld(a, o[2])) - f2(ld(a, o[5])));
+    }
+    __device__ __forceinline__ void grad(int a, f2& gx, f2& gy, f2& gz) const {
+        gx = dx(a);
+        gy = d1(a, oy);
+        gz = d1(a, oz);
+    }
+    __device__ __forceinline__ void grad_lap(int a, f2& gx, f2& gy, f2& gz, f2& lap) const {
+        f2 s1, s2, s3;
+        {
+            f2 p1, p2, p3, m1, m2, m3;
+            xpairs(a, p1, p2, p3, m1, m2, m3);
+            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            s1 = p1 + m1;
+            s2 = p2 + m2;
+            s3 = p3 + m3;
+        }
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            const int* o = ax == 0 ? oy : oz;
+            const f2 p1 = f2(ld(a, o[0])), p2 = f2(ld(a, o[1])), p3 = f2(ld(a, o[2]));
+            const f2 m1 = f2(ld(a, o[3])), m2 = f2(ld(a, o[4])), m3 = f2(ld(a, o[5]));
+            const f2 g = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            if (ax == 0)
+                gy = g;
+            else
+                gz = g;
+            s1 += p1 + m1;
+            s2 += p2 + m2;
+            s3 += p3 + m3;
+        }
+        lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
+    }
+    __device__ __forceinline__ f2 div3(int a) const { return dx(a) + d1(a + 1, oy) + d1(a + 2, oz); }
+
+    __device__ __forceinline__ void place(int i0, int j, int k, int nx, int ny, int nz) {
+        c = i0 + nx * (j + ny * k);
+        ox[0] = (i0 - 4 >= 0 ? -4 : nx - 4);
+        ox[1] = (i0 - 2 >= 0 ? -2 : nx - 2);
+        ox[2] = (i0 + 2 < nx ? 2 : 2 - nx);
+        ox[3] = (i0 + 4 < nx ? 4 : 4 - nx);
+        axis_offsets(j, ny, nx, oy);
+        axis_offsets(k, nz, nx * ny, oz);
+    }
+};
+
+template <typename T>
+__host__ __device__ inline StencilCoef<f2> pair_stencil(const StencilCoef<T>& s) {
+    return StencilCoef<f2>{f2(s.a1), f2(s.a2), f2(s.a3), f2(s.l0), f2(s.l1), f2(s.l2), f2(s.l3)};
+}
+
+// Compensated accumulation (hi, lo) += p (TwoSum, then renormalise).
+template <typename T>
+__device__ __forceinline__ void acc_hilo(T& hi, T& lo, T p) {
+    const T s = hi + p;
+    const T bp = s - hi;
+    const T e = (hi - (s - bp)) + (p - bp);
+    const T t = lo + e;
+    hi = s + t;
+    lo = t - (hi - s);
+}

@@ -235,7 +235,9 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         if (c->p.precision == EWPT_FP64)
             e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
         else
-            e = launch_step_fp32(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st);
+            e = (c->tile.pair && c->g.nx % 2 == 0)
+                    ? launch_step_fp32_pair(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st)
+                    : launch_step_fp32(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st);
         int rc = ewpt_cuda_check(c, e, "step launch");
         if (rc) return rc;
         c->it = it;
@@ -251,21 +253,24 @@ int ewpt_step_explicit(ewpt_ctx* c, int32_t nsteps, double Jex, double gamma) {
 
 int64_t ewpt_iteration(const ewpt_ctx* c) { return c ? c->it : -1; }
 
-int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg) {
+int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pair) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     if (reg < 0 || reg > 2) return ewpt_fail(c, EWPT_ERR_ARG, "register variant %d unknown (0..2)", reg);
     if (bx < 1 || by < 1 || bx * by > tiling_max_threads(reg) || (bx * by) % 32 != 0)
         return ewpt_fail(c, EWPT_ERR_ARG, "tile %dx%d: need whole warps and at most %d threads for variant %d", bx, by,
                          tiling_max_threads(reg), reg);
-    c->tile = Tiling{bx, by, reg};
+    if (pair != 0 && pair != 1) return ewpt_fail(c, EWPT_ERR_ARG, "pair must be 0 or 1");
+    if (pair && c->g.nx % 2 != 0) return ewpt_fail(c, EWPT_ERR_ARG, "paired sites need an even nx");
+    c->tile = Tiling{bx, by, reg, pair};
     return EWPT_OK;
 }
 
-int ewpt_get_tiling(const ewpt_ctx* c, int32_t* bx, int32_t* by, int32_t* reg) {
-    if (!c || !bx || !by || !reg) return ewpt_fail(nullptr, EWPT_ERR_ARG, "NULL argument");
+int ewpt_get_tiling(const ewpt_ctx* c, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair) {
+    if (!c || !bx || !by || !reg || !pair) return ewpt_fail(nullptr, EWPT_ERR_ARG, "NULL argument");
     *bx = c->tile.bx;
     *by = c->tile.by;
     *reg = c->tile.reg;
+    *pair = c->tile.pair;
     return EWPT_OK;
 }
 

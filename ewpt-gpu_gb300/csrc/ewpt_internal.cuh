@@ -94,13 +94,16 @@ cudaError_t launch_rates_fp64(const Grid& g, const Ptr36& in, const MPtr36& out,
 // plane per grid slice; reg selects the register-budget variant (stage.cu).
 struct Tiling {
     int bx, by, reg;
+    int pair;  // FP32 form: 1 = two x-adjacent sites per thread (stage_pair.cu), needs nx even
 };
-constexpr Tiling kDefaultTiling{32, 4, 0};
+constexpr Tiling kDefaultTiling{32, 4, 0, 0};
 int tiling_max_threads(int reg);
 
 cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
 cudaError_t launch_step_fp32(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
                              double Jex, double gam, cudaStream_t st);
+cudaError_t launch_step_fp32_pair(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
+                                  double Jex, double gam, cudaStream_t st);
 cudaError_t launch_fp32_split(const Grid& g, const double* src, Fp32State dst, cudaStream_t st);
 cudaError_t launch_fp32_join(const Grid& g, Fp32State src, double* dst, cudaStream_t st);

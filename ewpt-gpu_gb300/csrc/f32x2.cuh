@@ -14,11 +14,11 @@ struct Prod;
 
 struct f2 {
     float2 v;
-    __device__ __forceinline__ f2() {}
-    __device__ __forceinline__ f2(float2 x) : v(x) {}
-    __device__ __forceinline__ explicit f2(float s) : v(make_float2(s, s)) {}
-    __device__ __forceinline__ explicit f2(double s) : v(make_float2((float)s, (float)s)) {}
-    __device__ __forceinline__ explicit f2(int s) : v(make_float2((float)s, (float)s)) {}
+    __host__ __device__ __forceinline__ f2() {}
+    __host__ __device__ __forceinline__ f2(float2 x) : v(x) {}
+    __host__ __device__ __forceinline__ explicit f2(float s) : v(make_float2(s, s)) {}
+    __host__ __device__ __forceinline__ explicit f2(double s) : v(make_float2((float)s, (float)s)) {}
+    __host__ __device__ __forceinline__ explicit f2(int s) : v(make_float2((float)s, (float)s)) {}
     __device__ __forceinline__ f2(const Prod& p);
     __device__ __forceinline__ f2& operator+=(const f2& b);
     __device__ __forceinline__ f2& operator-=(const f2& b);

@@ -69,9 +69,9 @@ def _sig(L):
     L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_kc_bin_nums.restype = C.c_int64
     L.ewpt_diagnostics_noalloc.argtypes = [P, C.c_void_p, DP, C.c_void_p]
-    L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     I32P = C.POINTER(C.c_int32)
-    L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P]
+    L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]
 
 
 def load():

@@ -16,9 +16,12 @@ from . import _lib, ic
 from .lattice import Lattice
 from .params import Params
 
-CANDIDATES = [(32, 4, 0), (64, 2, 0), (32, 2, 0), (16, 8, 0), (128, 1, 0),
-              (32, 4, 1), (64, 2, 1), (32, 2, 1), (16, 8, 1),
-              (32, 4, 2), (64, 2, 2), (32, 2, 2), (16, 8, 2)]
+CANDIDATES = [(32, 4, 0, 0), (64, 2, 0, 0), (32, 2, 0, 0), (16, 8, 0, 0), (128, 1, 0, 0),
+              (32, 4, 1, 0), (64, 2, 1, 0), (32, 2, 1, 0), (16, 8, 1, 0),
+              (32, 4, 2, 0), (64, 2, 2, 0), (32, 2, 2, 0), (16, 8, 2, 0)]
+# FP32 form only: two sites per thread (needs even nx)
+PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (32, 1, 0, 1),
+                   (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1)]
 
 
 def cache_path() -> str:
@@ -71,7 +74,10 @@ def time_tiling(lat: Lattice, tile, steps: int = 2) -> float:
 
 def sweep(p: Params, steps: int = 2, candidates=None) -> list:
     """(tiling, seconds per step) for every candidate on a scratch lattice."""
-    candidates = candidates or CANDIDATES
+    if candidates is None:
+        candidates = list(CANDIDATES)
+        if int(p.precision) == _lib.FP32 and p.dims[0] % 2 == 0:
+            candidates += PAIR_CANDIDATES
     res = []
     with Lattice(p) as lat:
         lat.set_state(ic.bubbles_tanh(p.dims, p.dx, 4, seed=0))

@@ -93,13 +93,13 @@ class Lattice:
         return int(self.L.ewpt_stream(self.h) or 0)
 
     # ------------------------------------------------------------ tiling
-    def set_tiling(self, bx: int, by: int, reg: int = 0):
-        self._chk(self.L.ewpt_set_tiling(self.h, int(bx), int(by), int(reg)))
+    def set_tiling(self, bx: int, by: int, reg: int = 0, pair: int = 0):
+        self._chk(self.L.ewpt_set_tiling(self.h, int(bx), int(by), int(reg), int(pair)))
 
     def tiling(self) -> tuple:
-        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
-        self._chk(self.L.ewpt_get_tiling(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return (a.value, b.value, c.value)
+        a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        self._chk(self.L.ewpt_get_tiling(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return (a.value, b.value, c.value, d.value)
 
     # ------------------------------------------------------------ observables
     def diagnostics(self, allow_nonfinite: bool = False) -> np.ndarray:

@@ -103,10 +103,13 @@ int ewpt_step_explicit(ewpt_ctx* ctx, int32_t nsteps, double Jex, double gamma);
 int64_t ewpt_iteration(const ewpt_ctx* ctx);
 /* Launch shape of the stage kernels: blocks of bx*by threads over x and y
  * (whole warps, at most 128 threads), reg = register-budget variant (0:
- * registers at the compiler's choice; 1: <= 128 registers; 2: <= 168).  Results do not depend on it; ewpt/autotune.py picks it per
- * lattice size and precision.  Default 32x4, variant 0. */
-int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg);
-int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg);
+ * registers at the compiler's choice; 1: <= 128 registers; 2: <= 168);
+ * pair = 1 (FP32 form, even nx): each thread evolves two x-adjacent sites
+ * with packed FP32x2 arithmetic.  The result of a step does not depend on
+ * bx, by or reg, and pair only changes FP32 rounding; ewpt/autotune.py
+ * picks the fastest per lattice size and precision.  Default 32x4, 0, 0. */
+int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg, int32_t pair);
+int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair);
 /* Wait for all work queued on the context. */
 int ewpt_sync(ewpt_ctx* ctx);
 /* The context's cudaStream_t, as an opaque pointer. */

@@ -176,6 +176,24 @@ def test_spectrum_unique_matches_convolve_1d_golden(golden_dir):
     np.testing.assert_allclose(s["mean"], g["spec"][:, 1], rtol=1e-10)
 
 
+@pytest.mark.parametrize("tile", [(32, 4, 0, 0), (32, 4, 0, 1), (64, 2, 2, 1)])
+def test_fp32_tilings_agree(tile):
+    """Every FP32 launch shape (incl. two sites per thread with packed FP32x2
+    arithmetic) gives the same evolution to FP32 round-off."""
+    shape = (32, 24, 20)
+    p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32, beta_w=0.2)
+    y0 = perturbed_bubbles(shape, p32.dx, 3, seed=8, amp=0.02)
+    res = []
+    for t in [(32, 4, 0, 0), tile]:
+        with ewpt.Lattice(p32) as lat:
+            lat.set_state(y0)
+            lat.set_tiling(*t)
+            assert lat.tiling() == t
+            lat.step(20)
+            res.append(lat.get_state())
+    assert rel_err(res[1], res[0]) < 2e-5
+
+
 def test_fp32_form_tracks_fp64():
     """FP32 form vs FP64 on a smooth bubble IC: fields within 1e-4 of FP64
     after 100 steps, energy drift and Gauss violation within 2x of FP64
@@ -185,20 +203,24 @@ def test_fp32_form_tracks_fp64():
     p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32)
     y0 = ewpt.ic.bubbles_tanh(shape, p64.dx, 4, seed=21)
     res = {}
-    for name, p in (("64", p64), ("32", p32)):
+    for name, p in (("64", p64), ("32", p32), ("32x2", p32)):
         with ewpt.Lattice(p) as lat:
             lat.set_state(y0)
+            if name == "32x2":
+                lat.set_tiling(32, 4, 0, 1)
             d0 = lat.diagnostics()
             lat.step(100)
             res[name] = (lat.get_state(), d0, lat.diagnostics(), lat.spectrum("B", "log", 12))
-    y64, y32 = res["64"][0], res["32"][0]
-    assert rel_err(y32[:20], y64[:20]) < 1e-4
+    y64 = res["64"][0]
     e0 = res["64"][1][13]
     drift64 = abs(res["64"][2][13] - e0)
-    drift32 = abs(res["32"][2][13] - e0)
-    assert drift32 <= 2.0 * drift64 + 1e-6 * abs(e0)
-    g64, g32 = res["64"][2][14], res["32"][2][14]
-    assert g32 <= 2.0 * g64 + 1e-6
-    s64, s32 = res["64"][3]["mean"], res["32"][3]["mean"]
+    g64 = res["64"][2][14]
+    s64 = res["64"][3]["mean"]
     m = s64 > 1e-12 * s64.max()
-    np.testing.assert_allclose(s32[m], s64[m], rtol=1e-4)
+    for name in ("32", "32x2"):
+        y32 = res[name][0]
+        assert rel_err(y32[:20], y64[:20]) < 1e-4
+        drift32 = abs(res[name][2][13] - e0)
+        assert drift32 <= 2.0 * drift64 + 1e-6 * abs(e0)
+        assert res[name][2][14] <= 2.0 * g64 + 1e-6
+        np.testing.assert_allclose(res[name][3]["mean"][m], s64[m], rtol=1e-4)

@@ -126,6 +126,26 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
     return EWPT_OK;
 }
 
+int ewpt_create_view(const ewpt_params* p, ewpt_ctx** out) {
+    int rc = ewpt_validate_params(p, nullptr);
+    if (rc) return rc;
+    ewpt_ctx* c = new ewpt_ctx();
+    c->p = *p;
+    c->p.precision = EWPT_FP64;
+    c->g = Grid{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz};
+    c->view = true;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->y, (size_t)36 * c->g.S * 8);
+    rc = ewpt_cuda_check(nullptr, e, "view allocation");
+    if (rc) {
+        ewpt_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return EWPT_OK;
+}
+
 int ewpt_destroy(ewpt_ctx* c) {
     if (!c) return EWPT_OK;
     cudaSetDevice(c->p.device);
@@ -223,6 +243,7 @@ static double damp_of(const ewpt_params& p, int64_t it) {
 
 static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double gam) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (c->view) return ewpt_fail(c, EWPT_ERR_STATE, "this context is a read-only view");
     if (nsteps < 0) return ewpt_fail(c, EWPT_ERR_ARG, "nsteps < 0");
     if (expl && (!std::isfinite(Jex) || !std::isfinite(gam)))
         return ewpt_fail(c, EWPT_ERR_ARG, "non-finite Jex/gamma");

@@ -10,6 +10,7 @@ struct ewpt_ctx {
     Grid g{};
     cudaStream_t st = nullptr;
     int64_t it = 0;  // RK4 iterations done (the reference's loop counter)
+    bool view = false;  // state buffer only (an ensemble member's FP64 view): no stepping
     Tiling tile = kDefaultTiling;  // stage-kernel launch shape
     // FP64 form: state y, accumulator yn, stage inputs xa/xb, each [36][S]
     double* y = nullptr;
@@ -36,8 +37,14 @@ struct ewpt_ctx {
 int ewpt_fail(ewpt_ctx* ctx, int code, const char* fmt, ...);
 int ewpt_cuda_check(ewpt_ctx* ctx, cudaError_t e, const char* what);
 int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx);
+// FP64 context holding only the state buffer, for diagnostics and spectra of
+// a state that lives elsewhere (ensemble members).
+extern "C" int ewpt_create_view(const ewpt_params* p, ewpt_ctx** out);
 // FP64 view of the current state: c->y for FP64 contexts; for FP32 contexts
 // the state joined into c->scratch64.
 int ewpt_state64(ewpt_ctx* c, const double** out);
 int ewpt_ensure_scratch64(ewpt_ctx* c);
 void ewpt_release_aux(ewpt_ctx* c);
+// Bubble IC kernel (init.cu) on an FP64 state (y) or an FP32 hi/lo state.
+int ewpt_launch_bubbles(const Grid& g, double dx, int nb, const double* bubbles, int profile, double p0, double p1,
+                        double p2, double* y, float* hi, float* lo, cudaStream_t st, std::string* err);

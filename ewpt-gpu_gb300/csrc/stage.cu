@@ -18,7 +18,7 @@
 //   stage 2, 3:  kacc += 2 k_s;       X3 = y_hi + k2 dt/2,  X4 = y_hi + k3 dt
 //   stage 4:     (y_hi, y_lo) += dt/6 (kacc + k4), compensated, in place
 // (X_1 is y_hi itself).  Bytes per site-update: FP64 4608, FP32 2736.
-#include "ewpt_internal.cuh"
+#include "accessors.cuh"
 
 namespace {
 
@@ -35,57 +35,8 @@ struct RegBudget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
 template <>
 struct RegBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
 
-// Stage input read from global memory through the read-only path.
 template <typename TL, typename T>
-struct GlobalAcc {
-    const Ptr36& P;
-    int c;
-    int ox[6], oy[6], oz[6];
-    StencilCoef<T> s;
-
-    __device__ __forceinline__ T ld(int a, int off) const {
-        return (T)__ldg(reinterpret_cast<const TL*>(P.p[a]) + (c + off));
-    }
-    __device__ __forceinline__ T v(int a) const { return ld(a, 0); }
-    __device__ __forceinline__ T d1(int a, const int* o) const {
-        return s.a1 * (ld(a, o[0]) - ld(a, o[3])) + s.a2 * (ld(a, o[1]) - ld(a, o[4])) +
-               s.a3 * (ld(a, o[2]) - ld(a, o[5]));
-    }
-    __device__ __forceinline__ void grad(int a, T& gx, T& gy, T& gz) const {
-        gx = d1(a, ox);
-        gy = d1(a, oy);
-        gz = d1(a, oz);
-    }
-    __device__ __forceinline__ void grad_lap(int a, T& gx, T& gy, T& gz, T& lap) const {
-        T s1 = T(0), s2 = T(0), s3 = T(0);
-        {
-            const T p1 = ld(a, ox[0]), p2 = ld(a, ox[1]), p3 = ld(a, ox[2]);
-            const T m1 = ld(a, ox[3]), m2 = ld(a, ox[4]), m3 = ld(a, ox[5]);
-            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-            s1 = p1 + m1;
-            s2 = p2 + m2;
-            s3 = p3 + m3;
-        }
-        {
-            const T p1 = ld(a, oy[0]), p2 = ld(a, oy[1]), p3 = ld(a, oy[2]);
-            const T m1 = ld(a, oy[3]), m2 = ld(a, oy[4]), m3 = ld(a, oy[5]);
-            gy = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-            s1 += p1 + m1;
-            s2 += p2 + m2;
-            s3 += p3 + m3;
-        }
-        {
-            const T p1 = ld(a, oz[0]), p2 = ld(a, oz[1]), p3 = ld(a, oz[2]);
-            const T m1 = ld(a, oz[3]), m2 = ld(a, oz[4]), m3 = ld(a, oz[5]);
-            gz = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-            s1 += p1 + m1;
-            s2 += p2 + m2;
-            s3 += p3 + m3;
-        }
-        lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
-    }
-    __device__ __forceinline__ T div3(int a) const { return d1(a, ox) + d1(a + 1, oy) + d1(a + 2, oz); }
-};
+using GlobalAcc = SiteAcc<TL, T, SrcPtr36<TL>>;
 
 template <typename TL, typename T>
 __device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc, GlobalAcc<TL, T>& A) {
@@ -93,10 +44,7 @@ __device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return false;
-    A.c = i + g.nx * (j + g.ny * k);
-    axis_offsets(i, g.nx, 1, A.ox);
-    axis_offsets(j, g.ny, g.nx, A.oy);
-    axis_offsets(k, g.nz, g.nx * g.ny, A.oz);
+    A.place(i, j, k, g.nx, g.ny, g.nz);
     A.s = sc;
     return true;
 }
@@ -112,7 +60,7 @@ template <bool BETA>
 __global__ void __launch_bounds__(256) k_rates_fp64(Grid g, const __grid_constant__ Ptr36 X,
                                                        const __grid_constant__ MPtr36 R, PhysCoef<double> pc,
                                                        StencilCoef<double> sc) {
-    GlobalAcc<double, double> A{X};
+    GlobalAcc<double, double> A{{X}};
     if (!make_acc(g, sc, A)) return;
     RatesSink out{R, A.c};
     site_rates<double, BETA>(A, pc, out);
@@ -151,23 +99,13 @@ __global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMin
                                                        double* __restrict__ xn, double* acc_out,
                                                        PhysCoef<double> pc, StencilCoef<double> sc, double w,
                                                        double h) {
-    GlobalAcc<double, double> A{X};
+    GlobalAcc<double, double> A{{X}};
     if (!make_acc(g, sc, A)) return;
     Fp64Sink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};
     site_rates<double, BETA>(A, pc, out);
 }
 
 // ------------------------------------------------------------- FP32 stage
-// Compensated accumulation (hi, lo) += p (TwoSum, then renormalise).
-__device__ __forceinline__ void acc2(float& hi, float& lo, float p) {
-    const float s = hi + p;
-    const float bp = s - hi;
-    const float e = (hi - (s - bp)) + (p - bp);
-    const float t = lo + e;
-    hi = s + t;
-    lo = t - (hi - s);
-}
-
 struct Fp32Bufs {
     float* yhi;  // [36][S] state, high part (also the stage-1 stencil input)
     float* ylo;  // [36][S] state, low part
@@ -194,7 +132,7 @@ struct Fp32Sink {
         } else {
             const float s = __ldg(b.kacc + q) + r;
             float hi = __ldg(b.yhi + q), lo = __ldg(b.ylo + q);
-            acc2(hi, lo, w6 * s);
+            acc_hilo(hi, lo, w6 * s);
             b.yhi[q] = hi;
             b.ylo[q] = lo;
         }
@@ -205,7 +143,7 @@ template <int STAGE, bool BETA, int REG>
 __global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks) k_stage_fp32(Grid g, const __grid_constant__ Ptr36 X, Fp32Bufs b,
                                                        float* __restrict__ xn, PhysCoef<float> pc,
                                                        StencilCoef<float> sc, float h, float w6) {
-    GlobalAcc<float, float> A{X};
+    GlobalAcc<float, float> A{{X}};
     if (!make_acc(g, sc, A)) return;
     Fp32Sink<STAGE> out{A, b, xn, g.S, h, w6};
     site_rates<float, BETA>(A, pc, out);

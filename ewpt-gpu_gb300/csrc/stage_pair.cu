@@ -8,8 +8,7 @@
 // float2 loads) are re-paired into the +-1, +-2, +-3 neighbour pairs; y and z
 // neighbours are aligned float2 loads of the same x pair.  Needs nx even
 // (a pair never straddles the periodic wrap).
-#include "ewpt_internal.cuh"
-#include "f32x2.cuh"
+#include "accessors.cuh"
 
 namespace {
 
@@ -22,77 +21,6 @@ struct PairBudget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
 template <>
 struct PairBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
 
-struct PairAcc {
-    const Ptr36& P;
-    int c;        // linear index of site i0 (even)
-    int ox[4];    // float offsets of the x pairs at i0-4, i0-2, i0+2, i0+4 (wrapped)
-    int oy[6], oz[6];
-    StencilCoef<f2> s;
-
-    __device__ __forceinline__ float2 ld(int a, int off) const {
-        return __ldg(reinterpret_cast<const float2*>(reinterpret_cast<const float*>(P.p[a]) + (c + off)));
-    }
-    __device__ __forceinline__ f2 v(int a) const { return f2(ld(a, 0)); }
-    // x-neighbour pairs of the two sites: p1 = (f[i0+1], f[i0+2]) ... m3 = (f[i0-3], f[i0-2])
-    __device__ __forceinline__ void xpairs(int a, f2& p1, f2& p2, f2& p3, f2& m1, f2& m2, f2& m3) const {
-        const float2 qm2 = ld(a, ox[0]), qm1 = ld(a, ox[1]), q0 = ld(a, 0), qp1 = ld(a, ox[2]), qp2 = ld(a, ox[3]);
-        p1 = f2(make_float2(q0.y, qp1.x));
-        p2 = f2(qp1);
-        p3 = f2(make_float2(qp1.y, qp2.x));
-        m1 = f2(make_float2(qm1.y, q0.x));
-        m2 = f2(qm1);
-        m3 = f2(make_float2(qm2.y, qm1.x));
-    }
-    __device__ __forceinline__ f2 dx(int a) const {
-        f2 p1, p2, p3, m1, m2, m3;
-        xpairs(a, p1, p2, p3, m1, m2, m3);
-        return s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-    }
-    __device__ __forceinline__ f2 d1(int a, const int* o) const {
-        return s.a1 * (f2(ld(a, o[0])) - f2(ld(a, o[3]))) + s.a2 * (f2(ld(a, o[1])) - f2(ld(a, o[4]))) +
-               s.a3 * (f2(ld(a, o[2])) - f2(ld(a, o[5])));
-    }
-    __device__ __forceinline__ void grad(int a, f2& gx, f2& gy, f2& gz) const {
-        gx = dx(a);
-        gy = d1(a, oy);
-        gz = d1(a, oz);
-    }
-    __device__ __forceinline__ void grad_lap(int a, f2& gx, f2& gy, f2& gz, f2& lap) const {
-        f2 s1, s2, s3;
-        {
-            f2 p1, p2, p3, m1, m2, m3;
-            xpairs(a, p1, p2, p3, m1, m2, m3);
-            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-            s1 = p1 + m1;
-            s2 = p2 + m2;
-            s3 = p3 + m3;
-        }
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax) {
-            const int* o = ax == 0 ? oy : oz;
-            const f2 p1 = f2(ld(a, o[0])), p2 = f2(ld(a, o[1])), p3 = f2(ld(a, o[2]));
-            const f2 m1 = f2(ld(a, o[3])), m2 = f2(ld(a, o[4])), m3 = f2(ld(a, o[5]));
-            const f2 g = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
-            if (ax == 0) gy = g; else gz = g;
-            s1 += p1 + m1;
-            s2 += p2 + m2;
-            s3 += p3 + m3;
-        }
-        lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
-    }
-    __device__ __forceinline__ f2 div3(int a) const { return dx(a) + d1(a + 1, oy) + d1(a + 2, oz); }
-};
-
-// Compensated accumulation on both lanes (TwoSum, then renormalise).
-__device__ __forceinline__ void acc2x2(f2& hi, f2& lo, f2 p) {
-    const f2 s = hi + p;
-    const f2 bp = s - hi;
-    const f2 e = (hi - (s - bp)) + (p - bp);
-    const f2 t = lo + e;
-    hi = s + t;
-    lo = t - (hi - s);
-}
-
 struct PairBufs {
     float* yhi;
     float* ylo;
@@ -101,7 +29,7 @@ struct PairBufs {
 
 template <int STAGE>
 struct PairSink {
-    const PairAcc& A;
+    const PairAcc<SrcPtr36<float>>& A;
     PairBufs b;
     float* __restrict__ xn;
     int64_t S;
@@ -122,7 +50,7 @@ struct PairSink {
         } else {
             const f2 s = f2(rd(b.kacc, q)) + r;
             f2 hi(rd(b.yhi, q)), lo(rd(b.ylo, q));
-            acc2x2(hi, lo, f2(w6 * s));
+            acc_hilo(hi, lo, f2(w6 * s));
             *at(b.yhi, q) = hi.v;
             *at(b.ylo, q) = lo.v;
         }
@@ -138,22 +66,11 @@ __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kM
     const int k = blockIdx.z;
     const int i0 = 2 * ip;
     if (i0 >= g.nx || j >= g.ny) return;
-    PairAcc A{X};
-    A.c = i0 + g.nx * (j + g.ny * k);
-    A.ox[0] = (i0 - 4 >= 0 ? -4 : g.nx - 4);
-    A.ox[1] = (i0 - 2 >= 0 ? -2 : g.nx - 2);
-    A.ox[2] = (i0 + 2 < g.nx ? 2 : 2 - g.nx);
-    A.ox[3] = (i0 + 4 < g.nx ? 4 : 4 - g.nx);
-    axis_offsets(j, g.ny, g.nx, A.oy);
-    axis_offsets(k, g.nz, g.nx * g.ny, A.oz);
+    PairAcc<SrcPtr36<float>> A{{X}};
+    A.place(i0, j, k, g.nx, g.ny, g.nz);
     A.s = sc;
     PairSink<STAGE> out{A, b, xn, g.S, h, w6};
     site_rates<f2, BETA>(A, pc, out);
-}
-
-template <typename T>
-StencilCoef<f2> pair_stencil(const StencilCoef<T>& s) {
-    return StencilCoef<f2>{f2(s.a1), f2(s.a2), f2(s.a3), f2(s.l0), f2(s.l1), f2(s.l2), f2(s.l3)};
 }
 
 Ptr36 pack4(const void* base, int64_t S) {

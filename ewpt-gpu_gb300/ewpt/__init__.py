@@ -7,8 +7,9 @@ its C ABI (include/ewpt.h).
 """
 from . import _lib, ic
 from ._lib import FP32, FP64, EwptError, load
+from .ensemble import Ensemble
 from .lattice import DIAG_NAMES, Lattice, kc_bin_nums, rk4_rates_device
 from .params import Params, baseline_couplings
 
-__all__ = ["Lattice", "Params", "baseline_couplings", "ic", "FP32", "FP64", "EwptError", "load",
+__all__ = ["Ensemble", "Lattice", "Params", "baseline_couplings", "ic", "FP32", "FP64", "EwptError", "load",
            "DIAG_NAMES", "kc_bin_nums", "rk4_rates_device", "_lib"]

@@ -20,6 +20,7 @@ NDIAG = 20
 OK, ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_STATE = range(8)
 FP64, FP32 = 0, 1
 FIELD_B, FIELD_B2, FIELD_HIGGS = 0, 1, 2
+BUBBLE_REFERENCE, BUBBLE_TANH = 0, 1
 SPEC_LOG, SPEC_UNIQUE = 0, 1
 
 
@@ -69,6 +70,28 @@ def _sig(L):
     L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_kc_bin_nums.restype = C.c_int64
     L.ewpt_diagnostics_noalloc.argtypes = [P, C.c_void_p, DP, C.c_void_p]
+    E = C.c_void_p
+    L.ewpt_ensemble_create.argtypes = [C.c_int32, C.POINTER(EwptParams), C.POINTER(E)]
+    L.ewpt_ensemble_destroy.argtypes = [E]
+    L.ewpt_ensemble_last_error.argtypes = [E]
+    L.ewpt_ensemble_last_error.restype = C.c_char_p
+    L.ewpt_ensemble_size.argtypes = [E]
+    L.ewpt_ensemble_size.restype = C.c_int32
+    L.ewpt_ensemble_sites.argtypes = [E]
+    L.ewpt_ensemble_sites.restype = C.c_int64
+    L.ewpt_ensemble_set_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
+    L.ewpt_ensemble_get_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
+    L.ewpt_ensemble_set_drive.argtypes = [E, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_ensemble_set_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_ensemble_step.argtypes = [E, C.c_int32]
+    L.ewpt_ensemble_sync.argtypes = [E]
+    L.ewpt_ensemble_stream.argtypes = [E]
+    L.ewpt_ensemble_stream.restype = C.c_void_p
+    L.ewpt_ensemble_diagnostics.argtypes = [E, C.c_int32, DP]
+    L.ewpt_ensemble_spectrum.argtypes = [E, C.c_int32, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP,
+                                         C.POINTER(C.c_int32)]
+    L.ewpt_init_bubbles.argtypes = [V, C.c_int32, DP, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_ensemble_init_bubbles.argtypes = [E, C.c_int32, C.c_int32, DP, C.c_int32, C.c_double, C.c_double]
     L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     I32P = C.POINTER(C.c_int32)
     L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]

@@ -90,16 +90,32 @@ def bubbles_reference(p: Params, nbub: int | None = None, seed: int | None = Non
     return y
 
 
-def bubbles_tanh(shape, dx, nbub, lam=0.129, vev=1.0, seed=0, radius=None, width=None):
-    """Benchmark bubble IC: nbub seeded bubbles, tanh core of radius 2/sqrt(lam)."""
+def tanh_bubble_list(shape, dx, nbub, seed=0) -> np.ndarray:
+    """(nbub, 7): seeded uniform centres (physical units) and directions
+    uniform on S^3 -- the draws of bubbles_tanh, for ewpt_init_bubbles."""
     rng = np.random.default_rng(seed)
-    R = 2.0 / math.sqrt(lam) if radius is None else radius
-    w = 1.0 / (math.sqrt(lam) * vev) if width is None else width
     nx, ny, nz = shape
     L = np.array([nx * dx, ny * dx, nz * dx])
     centres = rng.random((nbub, 3)) * L
     dirs = rng.normal(size=(nbub, 4))
     dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    return np.ascontiguousarray(np.hstack([centres, dirs]))
+
+
+def tanh_profile_params(lam=0.129, vev=1.0, radius=None, width=None):
+    """(R, w) of the benchmark bubble profile: R = 2/sqrt(lam), w = 1/(sqrt(lam) vev)."""
+    R = 2.0 / math.sqrt(lam) if radius is None else radius
+    w = 1.0 / (math.sqrt(lam) * vev) if width is None else width
+    return R, w
+
+
+def bubbles_tanh(shape, dx, nbub, lam=0.129, vev=1.0, seed=0, radius=None, width=None):
+    """Benchmark bubble IC: nbub seeded bubbles, tanh core of radius 2/sqrt(lam)."""
+    R, w = tanh_profile_params(lam, vev, radius, width)
+    nx, ny, nz = shape
+    L = np.array([nx * dx, ny * dx, nz * dx])
+    bl = tanh_bubble_list(shape, dx, nbub, seed)
+    centres, dirs = bl[:, :3], bl[:, 3:]
     x = np.arange(nx) * dx
     yv = np.arange(ny) * dx
     z = np.arange(nz) * dx

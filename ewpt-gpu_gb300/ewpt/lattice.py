@@ -101,6 +101,14 @@ class Lattice:
         self._chk(self.L.ewpt_get_tiling(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return (a.value, b.value, c.value, d.value)
 
+    # ------------------------------------------------------------ initial conditions
+    def init_bubbles(self, bubbles: np.ndarray, profile: str = "tanh", radius: float = 0.0, width: float = 0.0):
+        """Device bubble IC (ewpt_init_bubbles): bubbles is (nb, 7)."""
+        b = np.ascontiguousarray(bubbles, dtype=np.float64).reshape(-1, 7)
+        prof = _lib.BUBBLE_TANH if profile == "tanh" else _lib.BUBBLE_REFERENCE
+        self._chk(self.L.ewpt_init_bubbles(self.h, len(b), b.ctypes.data_as(_lib.DP), prof, float(radius),
+                                           float(width)))
+
     # ------------------------------------------------------------ observables
     def diagnostics(self, allow_nonfinite: bool = False) -> np.ndarray:
         out = np.zeros(_lib.NDIAG)

@@ -162,6 +162,55 @@ int ewpt_spectrum(ewpt_ctx* ctx, int32_t field, int32_t mode, int32_t nbins, dou
  * spec_routines.jl:32-43), -1 on bad input. */
 int64_t ewpt_kc_bin_nums(int32_t cx, int32_t cy, int32_t cz);
 
+enum ewpt_bubble_profile { EWPT_BUBBLE_REFERENCE = 0, EWPT_BUBBLE_TANH = 1 };
+
+/* Bubble-nucleation initial condition on the device (replaces the per-bubble
+ * initializer! launches, main_rk4.jl:4930-4946 and :5691-5697): phi_a =
+ * sum_b d_ab * profile_b(x), every other array zero, iteration counter reset.
+ * bubbles: nb rows of 7 doubles (centre cx, cy, cz, direction d1..d4).
+ * EWPT_BUBBLE_REFERENCE: the reference's rmag(rb) profile with its
+ *   sin-distance, centres in its 1-based site indices, mass = params.mH
+ *   (p0, p1 unused).
+ * EWPT_BUBBLE_TANH: vev * 0.5 * (1 - tanh((r - p0)/p1)), centres in physical
+ *   units, r the minimum-image distance (p0 = radius, p1 = wall width). */
+int ewpt_init_bubbles(ewpt_ctx* ctx, int32_t nb, const double* bubbles, int32_t profile, double p0, double p1);
+
+/* ---------------------------------------------------------------------
+ * Batched ensembles (no counterpart in the reference, which runs one
+ * realization per process; each member here is an independent lattice with
+ * its own size, couplings and dt, in the FP32 form).  One RK4 stage over all
+ * members is one persistent kernel launch; the four stages of a step are
+ * replayed from a CUDA graph.  Member m evolves exactly like a single
+ * FP32-form context with the same paired/scalar mode.  Members start at
+ * zero and carry per-member Jex/gamma (default 0, see ewpt_ensemble_set_drive).
+ */
+typedef struct ewpt_ens ewpt_ens;
+int ewpt_ensemble_create(int32_t n, const ewpt_params* members, ewpt_ens** out);
+int ewpt_ensemble_destroy(ewpt_ens* ens);
+const char* ewpt_ensemble_last_error(const ewpt_ens* ens);
+int32_t ewpt_ensemble_size(const ewpt_ens* ens);
+/* total lattice sites over all members */
+int64_t ewpt_ensemble_sites(const ewpt_ens* ens);
+/* packed [36][S_m] FP64 state of member m, host (on_device = 0) or device memory */
+int ewpt_ensemble_set_state(ewpt_ens* ens, int32_t m, const double* packed, int32_t on_device);
+int ewpt_ensemble_get_state(ewpt_ens* ens, int32_t m, double* packed, int32_t on_device);
+/* ewpt_init_bubbles for member m */
+int ewpt_ensemble_init_bubbles(ewpt_ens* ens, int32_t m, int32_t nb, const double* bubbles, int32_t profile,
+                               double p0, double p1);
+/* constant Jex and gamma of member m for the following steps */
+int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
+/* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent
+ * sites per thread (every member needs an even nx; default when possible) */
+int ewpt_ensemble_set_tiling(ewpt_ens* ens, int32_t bx, int32_t by, int32_t pair);
+/* nsteps RK4 steps of every member, asynchronous on the ensemble's stream */
+int ewpt_ensemble_step(ewpt_ens* ens, int32_t nsteps);
+int ewpt_ensemble_sync(ewpt_ens* ens);
+void* ewpt_ensemble_stream(ewpt_ens* ens);
+/* ewpt_diagnostics / ewpt_spectrum of member m */
+int ewpt_ensemble_diagnostics(ewpt_ens* ens, int32_t m, double out[EWPT_NDIAG]);
+int ewpt_ensemble_spectrum(ewpt_ens* ens, int32_t m, int32_t field, int32_t mode, int32_t nbins, double* k,
+                           double* sum, double* count, double* mean, int32_t* nbins_out);
+
 /* Snapshot diagnostics (the same 20 columns as ewpt_diagnostics) of a
  * caller-owned FP64 state, without allocating any device memory.  No
  * counterpart in the reference: it is for callers that cannot let the

@@ -224,3 +224,31 @@ def test_fp32_form_tracks_fp64():
         assert drift32 <= 2.0 * drift64 + 1e-6 * abs(e0)
         assert res[name][2][14] <= 2.0 * g64 + 1e-6
         np.testing.assert_allclose(res[name][3]["mean"][m], s64[m], rtol=1e-4)
+
+
+@pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32])
+def test_device_bubble_ic_matches_host(prec):
+    shape = (24, 20, 18)
+    p = ewpt.baseline_couplings(shape=shape, N=24, dx=0.25, dt=0.025, precision=prec)
+    bl = ewpt.ic.tanh_bubble_list(shape, p.dx, 5, seed=12)
+    R, w = ewpt.ic.tanh_profile_params(p.lam, p.vev)
+    host = ewpt.ic.bubbles_tanh(shape, p.dx, 5, lam=p.lam, vev=p.vev, seed=12)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(np.ones((36, p.sites)))  # must be overwritten everywhere
+        lat.init_bubbles(bl, "tanh", R, w)
+        dev = lat.get_state()
+    np.testing.assert_allclose(dev, host, rtol=0, atol=1e-14)
+
+
+def test_device_reference_bubble_ic_matches_oracle():
+    shape = (20, 20, 20)
+    p = ewpt.baseline_couplings(shape=shape, N=20, dx=0.5, dt=0.05)
+    bl = np.array([[3, 5, 2, 0.5, -0.3, 0.7, 0.1], [16, 12, 7, -0.2, 0.9, 0.1, -0.4]], dtype=np.float64)
+    op = oparams(p)
+    yo = np.zeros((36, p.sites))
+    for b in bl:
+        orc.bubble_rmag(op, yo, b[:3], b[3:], p.mH)
+    with ewpt.Lattice(p) as lat:
+        lat.init_bubbles(bl, "reference")
+        dev = lat.get_state()
+    np.testing.assert_allclose(dev, yo, rtol=1e-13, atol=1e-15)

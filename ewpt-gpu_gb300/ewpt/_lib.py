@@ -92,6 +92,18 @@ def _sig(L):
                                          C.POINTER(C.c_int32)]
     L.ewpt_init_bubbles.argtypes = [V, C.c_int32, DP, C.c_int32, C.c_double, C.c_double]
     L.ewpt_ensemble_init_bubbles.argtypes = [E, C.c_int32, C.c_int32, DP, C.c_int32, C.c_double, C.c_double]
+    FP = C.POINTER(C.c_float)
+    L.ewpt_mlp_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(V)]
+    L.ewpt_mlp_destroy.argtypes = [V]
+    L.ewpt_mlp_last_error.argtypes = [V]
+    L.ewpt_mlp_last_error.restype = C.c_char_p
+    L.ewpt_mlp_num_params.argtypes = [V]
+    L.ewpt_mlp_num_params.restype = C.c_int64
+    L.ewpt_mlp_set_params.argtypes = [V, FP]
+    L.ewpt_mlp_get_params.argtypes = [V, FP]
+    L.ewpt_mlp_forward.argtypes = [V, FP, C.c_int32, FP]
+    L.ewpt_mlp_gradients.argtypes = [V, FP, FP, C.c_int32, FP, FP]
+    L.ewpt_mlp_train_step.argtypes = [V, FP, FP, C.c_int32, C.c_float, C.c_float, FP]
     L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     I32P = C.POINTER(C.c_int32)
     L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]

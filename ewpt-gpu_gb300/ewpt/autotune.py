@@ -107,3 +107,47 @@ def tune(lat: Lattice, steps: int = 2) -> tuple:
     tile = best_tiling(lat.params, steps)
     lat.set_tiling(*tile)
     return tile
+
+
+ENSEMBLE_CANDIDATES = [(32, 4, 1), (32, 2, 1), (64, 2, 1), (32, 1, 1), (32, 4, 0), (64, 2, 0), (32, 2, 0)]
+
+
+def best_ensemble_tiling(members, steps: int = 2, use_cache: bool = True) -> tuple:
+    """Fastest (bx, by, pair) for an ensemble of these members, timed on a
+    scratch ensemble (so no live state is touched) and cached by the member
+    shapes, couplings switches and GPU name."""
+    import hashlib
+
+    import torch
+
+    from .ensemble import Ensemble
+
+    shapes = ",".join(f"{p.dims[0]}x{p.dims[1]}x{p.dims[2]}" for p in members)
+    beta = int(any(p.beta_w != 0.0 or p.beta_y != 0.0 for p in members))
+    key = "ens:" + hashlib.sha1(shapes.encode()).hexdigest()[:16] + f":b{beta}:{torch.cuda.get_device_name(0)}"
+    cache = _load_cache() if use_cache else {}
+    if key in cache:
+        return tuple(cache[key]["tile"])
+    even = all(p.dims[0] % 2 == 0 for p in members)
+    res = []
+    with Ensemble(members) as ens:
+        for m, p in enumerate(members):
+            R, w = ic.tanh_profile_params(p.lam, p.vev)
+            ens.init_bubbles(m, ic.tanh_bubble_list(p.dims, p.dx, 4, seed=m), "tanh", R, w)
+        st = torch.cuda.ExternalStream(ens.stream)
+        for t in ENSEMBLE_CANDIDATES:
+            if t[2] and not even:
+                continue
+            ens.set_tiling(*t)
+            ens.step(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            ens.step(steps)
+            e1.record(st)
+            ens.sync()
+            res.append((t, e0.elapsed_time(e1) / 1e3 / steps))
+    tile, s = min(res, key=lambda r: r[1])
+    cache[key] = {"tile": list(tile), "s_per_step": s, "sweep": [[list(a), b] for a, b in res]}
+    if use_cache:
+        _save_cache(cache)
+    return tile

@@ -1,0 +1,38 @@
+"""Small profiling case for the stage kernels (one RK4 step per form/tiling).
+
+    python -m ewpt.prof_case [N] [--forms fp64,fp32,fp32x2]
+
+Builds an N^3 lattice (default 80: 512,000 sites, larger than L2 in every
+form) with 8 seeded tanh bubbles and runs one RK4 step in each requested
+form: fp64 (k_stage_fp64), fp32 (k_stage_fp32, 64x2 tiles, <=168 registers)
+and fp32x2 (k_stage_fp32x2, two sites per thread, 32x1 tiles).  Meant to be
+wrapped by ncu with -k regex:k_stage.
+"""
+import argparse
+
+from . import _lib, ic
+from .lattice import Lattice
+from .params import baseline_couplings
+
+TILES = {"fp64": (_lib.FP64, (32, 2, 0, 0)), "fp32": (_lib.FP32, (64, 2, 2, 0)), "fp32x2": (_lib.FP32, (32, 1, 0, 1))}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("N", nargs="?", type=int, default=80)
+    ap.add_argument("--forms", default="fp64,fp32,fp32x2")
+    a = ap.parse_args(argv)
+    for form in a.forms.split(","):
+        prec, tile = TILES[form]
+        p = baseline_couplings(N=a.N, dx=0.25, dt=0.025, precision=prec)
+        with Lattice(p) as lat:
+            R, w = ic.tanh_profile_params(p.lam, p.vev)
+            lat.init_bubbles(ic.tanh_bubble_list(p.dims, p.dx, 8, seed=1), "tanh", R, w)
+            lat.set_tiling(*tile)
+            lat.step(1)
+            lat.sync()
+    print("ok")
+
+
+if __name__ == "__main__":
+    main()

@@ -211,6 +211,30 @@ int ewpt_ensemble_diagnostics(ewpt_ens* ens, int32_t m, double out[EWPT_NDIAG]);
 int ewpt_ensemble_spectrum(ewpt_ens* ens, int32_t m, int32_t field, int32_t mode, int32_t nbins, double* k,
                            double* sum, double* count, double* mean, int32_t* nbins_out);
 
+/* ---------------------------------------------------------------------
+ * Learned surrogate (no counterpart in the reference): a 3-layer BF16 MLP
+ * n_in -> width -> width -> n_out with GELU, FP32 accumulation on the tensor
+ * cores, trained with AdamW on the GPU.  Parameters are FP32, flattened as
+ * W1 [width][n_in], b1 [width], W2 [width][width], b2 [width],
+ * W3 [n_out][width], b3 [n_out].  Inputs x [batch][n_in] and targets
+ * y [batch][n_out] are FP32 host arrays; the loss is the mean squared error.
+ */
+typedef struct ewpt_mlp ewpt_mlp;
+int ewpt_mlp_create(int32_t n_in, int32_t width, int32_t n_out, int32_t max_batch, int32_t device, ewpt_mlp** out);
+int ewpt_mlp_destroy(ewpt_mlp* net);
+const char* ewpt_mlp_last_error(const ewpt_mlp* net);
+int64_t ewpt_mlp_num_params(const ewpt_mlp* net);
+/* set (resets the optimizer state) / get the FP32 parameters */
+int ewpt_mlp_set_params(ewpt_mlp* net, const float* params);
+int ewpt_mlp_get_params(ewpt_mlp* net, float* params);
+/* y = net(x) */
+int ewpt_mlp_forward(ewpt_mlp* net, const float* x, int32_t batch, float* y);
+/* loss and d loss / d params (same layout as the parameters) at the current parameters */
+int ewpt_mlp_gradients(ewpt_mlp* net, const float* x, const float* y, int32_t batch, float* grads, float* loss);
+/* one AdamW step (beta1 0.9, beta2 0.999, eps 1e-8, decoupled weight decay); loss may be NULL */
+int ewpt_mlp_train_step(ewpt_mlp* net, const float* x, const float* y, int32_t batch, float lr, float weight_decay,
+                        float* loss);
+
 /* Snapshot diagnostics (the same 20 columns as ewpt_diagnostics) of a
  * caller-owned FP64 state, without allocating any device memory.  No
  * counterpart in the reference: it is for callers that cannot let the

@@ -252,3 +252,26 @@ def test_device_reference_bubble_ic_matches_oracle():
         lat.init_bubbles(bl, "reference")
         dev = lat.get_state()
     np.testing.assert_allclose(dev, yo, rtol=1e-13, atol=1e-15)
+
+
+def test_driver_energy_table_matches_oracle(tmp_path):
+    """ewpt.run (the run() driver mirror): the energy table every dsnaps steps
+    equals the oracle evolving the same reference-placement bubble IC."""
+    from ewpt import run as drv
+
+    args = ["0.0", "4", "20", "0.25", "10", "32", "0.99", "4", "0.0", "0.0", "0.0", "2"]
+    p = ewpt.Params.from_args(args)
+    res = drv.run(p, out_dir=str(tmp_path), nshell=12, verbose=False)
+    assert res["energies"].shape == (5, 13) and res["iterations"] == 20
+    assert (tmp_path / "energies.npy").exists()
+    op = oparams(p)
+    y = np.zeros((36, p.sites))
+    for b in drv.reference_bubble_list(p):
+        orc.bubble_rmag(op, y, b[:3], b[3:], p.mH)
+    rows = [orc.diagnostics(op, y)]
+    for _ in range(4):
+        y = orc.rk4_step(op, y, p.dt, 0.0, 0.0, nsteps=p.dsnaps)
+        rows.append(orc.diagnostics(op, y))
+    ref = np.array(rows)
+    np.testing.assert_allclose(res["energies"], ref[:, :13], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(res["total"], ref[:, 13], rtol=1e-9)

@@ -41,6 +41,12 @@ sys.path.insert(0, os.path.join(ROOT, "ewpt-gpu_gb300"))
 METRIC = "site-updates/s per RK4 step at 256³ (FP64 vs FP32 form), % of HBM peak"
 BYTES_FP64 = 3744  # 468 FP64 values per site-update (k-storage RK4)
 BYTES_FP32 = 2592  # y in FP64 width, stage rates in FP32
+# DRAM bytes per site-update (sum over the 4 stage launches) from one ncu
+# capture of the stage kernels at 80^3 (dram__bytes_read.sum +
+# dram__bytes_write.sum); traffic grows with the site count, so a 256^3
+# launch moves this x S / 4.
+TRAFFIC_FP64 = 4383
+TRAFFIC_FP32 = 2686
 N_BUBBLES = 64
 
 
@@ -152,11 +158,6 @@ def time_steps(lat, steps, warmup):
     return e0.elapsed_time(e1) / 1e3
 
 
-def time_stage_kernels(lat, steps):
-    """Average duration of one stage launch (4 per step), CUDA events."""
-    return None
-
-
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -254,9 +255,12 @@ def run_ours(args, ws, rank, local):
                    "parallelism": f"replicas x{ws}",
                    "tiling": {k: list(v) for k, v in tiles.items()}},
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_stage_fp64 (4 launches/step)",
+                     "traffic": TRAFFIC_FP64 * S / 4, "peak_kind": peak_kind,
+                     "kernel": "k_stage_fp64 (4 launches/step, the whole step)",
+                     "launch_ms": t64 / args.steps / 4 * 1e3,
+                     "traffic_source": "ncu dram bytes per site-update at 80^3 x sites / 4",
                      "algorithmic_bytes_per_site_update": BYTES_FP64,
-                     "note": "FP64 form is bound by the FP64 pipe, not HBM; see fp64_pipe in profiles/"},
+                     "note": "FP64 form is bound by the FP64 pipe (86% busy), not HBM"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }
@@ -274,6 +278,8 @@ def run_ours(args, ws, rank, local):
                             "speedup_vs_fp64": v32 / v,
                             "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm, "unit": "GB/s",
                                          "frac": a32 / hbm, "peak_kind": peak_kind,
+                                         "traffic": TRAFFIC_FP32 * S / 4,
+                                         "launch_ms": f["t"] / f["steps"] / 4 * 1e3,
                                          "algorithmic_bytes_per_site_update": BYTES_FP32}}
     if "ensemble" in res:
         out["ensemble"] = res["ensemble"]

@@ -79,6 +79,20 @@ struct SiteAcc {
         axis_offsets(j, ny, nx, oy);
         axis_offsets(k, nz, nx * ny, oz);
     }
+    // site (i, j, k) of a ghosted layout: the neighbours are plain strides
+    __device__ __forceinline__ void place_ghost(int i, int j, int k, const Layout& L) {
+        c = (int)L.at(i, j, k);
+        const int sy = L.px, sz = L.px * L.py;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            ox[d] = d + 1;
+            ox[d + 3] = -(d + 1);
+            oy[d] = (d + 1) * sy;
+            oy[d + 3] = -(d + 1) * sy;
+            oz[d] = (d + 1) * sz;
+            oz[d + 3] = -(d + 1) * sz;
+        }
+    }
 };
 
 // Two x-adjacent sites (i0, i0+1), i0 even, packed float pairs.  The x
@@ -156,6 +170,22 @@ struct PairAcc {
         ox[3] = (i0 + 4 < nx ? 4 : 4 - nx);
         axis_offsets(j, ny, nx, oy);
         axis_offsets(k, nz, nx * ny, oz);
+    }
+    // pair (i0, i0+1) of a ghosted layout
+    __device__ __forceinline__ void place_ghost(int i0, int j, int k, const Layout& L) {
+        c = (int)L.at(i0, j, k);
+        const int sy = L.px, sz = L.px * L.py;
+        ox[0] = -4;
+        ox[1] = -2;
+        ox[2] = 2;
+        ox[3] = 4;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            oy[d] = (d + 1) * sy;
+            oy[d + 3] = -(d + 1) * sy;
+            oz[d] = (d + 1) * sz;
+            oz[d + 3] = -(d + 1) * sz;
+        }
     }
 };
 

@@ -41,6 +41,9 @@ int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx) {
         return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large: nx*ny*nz must be < 2^31");
     if (p->precision != EWPT_FP64 && p->precision != EWPT_FP32)
         return ewpt_fail(ctx, EWPT_ERR_ARG, "precision %d unknown", p->precision);
+    if (p->precision == EWPT_FP32 &&
+        ghost_layout(Grid{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz}).P + 64 > (int64_t)INT32_MAX)
+        return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large for the FP32 form's padded arrays (< 2^31 cells)");
     const double v[] = {p->dx, p->dt, p->gw, p->gy, p->gp2, p->lambda, p->vev, p->theta_w,
                         p->beta_w, p->beta_y, p->gamma_inp, p->mH, p->t_sat};
     for (double x : v)
@@ -109,12 +112,16 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         if (e == cudaSuccess) e = cudaMalloc(&c->xb, n * 8);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->y, 0, n * 8, c->st);
     } else {
+        // ghosted layout; zero everything so the ghost cells no kernel writes
+        // (the box edges, never read by a stencil) hold finite values
+        c->lay = ghost_layout(c->g);
+        const size_t m = (size_t)36 * c->lay.P + 32;
         float** bufs[] = {&c->y32.hi, &c->y32.lo, &c->w32.kacc, &c->w32.xa, &c->w32.xb};
         e = cudaSuccess;
-        for (float** b : bufs)
-            if (e == cudaSuccess) e = cudaMalloc(b, n * 4);
-        if (e == cudaSuccess) e = cudaMemsetAsync(c->y32.hi, 0, n * 4, c->st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(c->y32.lo, 0, n * 4, c->st);
+        for (float** b : bufs) {
+            if (e == cudaSuccess) e = cudaMalloc(b, m * 4);
+            if (e == cudaSuccess) e = cudaMemsetAsync(*b, 0, m * 4, c->st);
+        }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     rc = ewpt_cuda_check(nullptr, e, "state allocation");
@@ -155,6 +162,7 @@ int ewpt_destroy(ewpt_ctx* c) {
     cudaFree(c->yn);
     cudaFree(c->xa);
     cudaFree(c->xb);
+    ewpt_tma_release(c);
     cudaFree(c->y32.hi);
     cudaFree(c->y32.lo);
     cudaFree(c->w32.kacc);
@@ -193,7 +201,7 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
     for (int a = 0; a < 36 && e == cudaSuccess; ++a)
         e = cudaMemcpyAsync(dst + (size_t)a * c->g.S, arrays[a], bytes,
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st);
-    if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, dst, c->y32, c->st);
+    if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, c->lay, dst, c->y32, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     return ewpt_cuda_check(c, e, "set_state");
 }
@@ -208,13 +216,14 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
     int rc = staging64(c, &src);
     if (rc) return rc;
     cudaError_t e = cudaSuccess;
-    if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->y32, src, c->st);
+    if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->lay, c->y32, src, c->st);
     const size_t bytes = (size_t)c->g.S * 8;
     for (int a = 0; a < 36 && e == cudaSuccess; ++a)
         e = cudaMemcpyAsync(arrays[a], src + (size_t)a * c->g.S, bytes,
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-    return ewpt_cuda_check(c, e, "get_state");
+    rc = ewpt_cuda_check(c, e, "get_state");
+    return rc ? rc : ewpt_tma_check(c);
 }
 
 int ewpt_set_state_packed(ewpt_ctx* c, const double* buf, int32_t on_device) {
@@ -255,10 +264,12 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         cudaError_t e;
         if (c->p.precision == EWPT_FP64)
             e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+        else if (c->tile.pair == 2)
+            e = launch_step_fp32_tma(c, J, G);
         else
             e = (c->tile.pair && c->g.nx % 2 == 0)
-                    ? launch_step_fp32_pair(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st)
-                    : launch_step_fp32(c->g, c->tile, c->y32, c->w32, c->p, J, G, c->st);
+                    ? launch_step_fp32_pair(c->g, c->lay, c->tile, c->y32, c->w32, c->p, J, G, c->st)
+                    : launch_step_fp32(c->g, c->lay, c->tile, c->y32, c->w32, c->p, J, G, c->st);
         int rc = ewpt_cuda_check(c, e, "step launch");
         if (rc) return rc;
         c->it = it;
@@ -276,11 +287,21 @@ int64_t ewpt_iteration(const ewpt_ctx* c) { return c ? c->it : -1; }
 
 int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pair) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (pair == 2) {
+        // TMA-staged shared-memory tiles of bx x by x reg sites (FP32 form)
+        if (bx != 32 || (by != 2 && by != 4) || reg != 4)
+            return ewpt_fail(c, EWPT_ERR_ARG, "TMA tiles: bx = 32, by in {2, 4}, reg (the z extent) = 4");
+        if (c->p.precision != EWPT_FP32) return ewpt_fail(c, EWPT_ERR_ARG, "TMA tiles need the FP32 form");
+        int rc = ewpt_tma_prepare(c, by, reg);
+        if (rc) return rc;
+        c->tile = Tiling{bx, by, reg, pair};
+        return EWPT_OK;
+    }
     if (reg < 0 || reg > 2) return ewpt_fail(c, EWPT_ERR_ARG, "register variant %d unknown (0..2)", reg);
     if (bx < 1 || by < 1 || bx * by > tiling_max_threads(reg) || (bx * by) % 32 != 0)
         return ewpt_fail(c, EWPT_ERR_ARG, "tile %dx%d: need whole warps and at most %d threads for variant %d", bx, by,
                          tiling_max_threads(reg), reg);
-    if (pair != 0 && pair != 1) return ewpt_fail(c, EWPT_ERR_ARG, "pair must be 0 or 1");
+    if (pair != 0 && pair != 1) return ewpt_fail(c, EWPT_ERR_ARG, "pair must be 0, 1 or 2");
     if (pair && c->g.nx % 2 != 0) return ewpt_fail(c, EWPT_ERR_ARG, "paired sites need an even nx");
     c->tile = Tiling{bx, by, reg, pair};
     return EWPT_OK;
@@ -298,7 +319,8 @@ int ewpt_get_tiling(const ewpt_ctx* c, int32_t* bx, int32_t* by, int32_t* reg, i
 int ewpt_sync(ewpt_ctx* c) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     cudaSetDevice(c->p.device);
-    return ewpt_cuda_check(c, cudaStreamSynchronize(c->st), "sync");
+    int rc = ewpt_cuda_check(c, cudaStreamSynchronize(c->st), "sync");
+    return rc ? rc : ewpt_tma_check(c);
 }
 
 void* ewpt_stream(ewpt_ctx* c) { return c ? (void*)c->st : nullptr; }

@@ -343,7 +343,7 @@ static int ens_view(ewpt_ens* e, int32_t m, ewpt_ctx** out) {
     if (ce == cudaSuccess) ce = cudaEventRecord(ev, e->st);
     if (ce == cudaSuccess) ce = cudaStreamWaitEvent(v->st, ev, 0);
     const EnsMember& M = e->tab[m];
-    if (ce == cudaSuccess) ce = launch_fp32_join(v->g, Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, v->y, v->st);
+    if (ce == cudaSuccess) ce = launch_fp32_join(v->g, plain_layout(v->g), Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, v->y, v->st);
     cudaEventDestroy(ev);
     int rc = ens_cuda(e, ce, "ensemble view");
     if (rc) return rc;
@@ -364,7 +364,7 @@ int ewpt_ensemble_set_state(ewpt_ens* e, int32_t m, const double* packed, int32_
     if (ce == cudaSuccess)
         ce = cudaMemcpyAsync(v->y, packed, (size_t)36 * M.S * 8,
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, e->st);
-    if (ce == cudaSuccess) ce = launch_fp32_split(v->g, v->y, Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, e->st);
+    if (ce == cudaSuccess) ce = launch_fp32_split(v->g, plain_layout(v->g), v->y, Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, e->st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
     return ens_cuda(e, ce, "ensemble set_state");
 }
@@ -444,7 +444,7 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* e, int32_t m, int32_t nb, const double*
     const Grid g{p.nx, p.ny, p.nz, M.S};
     std::string err;
     rc = ewpt_launch_bubbles(g, p.dx, nb, bubbles, profile, profile == EWPT_BUBBLE_REFERENCE ? p.mH : p0, p1, p.vev,
-                             nullptr, e->b.yhi + M.off, e->b.ylo + M.off, e->st, &err);
+                             nullptr, e->b.yhi + M.off, e->b.ylo + M.off, plain_layout(g), e->st, &err);
     if (rc) return ens_fail(e, rc, err.c_str());
     return EWPT_OK;
 }

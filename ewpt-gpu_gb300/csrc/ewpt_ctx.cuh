@@ -18,7 +18,9 @@ struct ewpt_ctx {
     double* xa = nullptr;
     double* xb = nullptr;
     // FP32 form: compensated state, weighted rate sum, float stage inputs
-    Fp32State y32{nullptr, nullptr};
+    Fp32State y32{nullptr, nullptr};  // all five FP32 buffers: [36][lay.P]
+    Layout lay{};
+    void* tma = nullptr;  // TMA stage-kernel state (stage_tma.cu), made by the first TMA tiling
     Fp32Work w32{nullptr, nullptr, nullptr};
     // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
     double* scratch64 = nullptr;
@@ -46,5 +48,13 @@ int ewpt_state64(ewpt_ctx* c, const double** out);
 int ewpt_ensure_scratch64(ewpt_ctx* c);
 void ewpt_release_aux(ewpt_ctx* c);
 // Bubble IC kernel (init.cu) on an FP64 state (y) or an FP32 hi/lo state.
+// TMA-staged FP32 stage kernels (stage_tma.cu).
+bool tma_tiling_fits(const Grid& g, int by, int bz);
+int ewpt_tma_prepare(ewpt_ctx* c, int by, int bz);
+void ewpt_tma_release(ewpt_ctx* c);
+int ewpt_tma_check(ewpt_ctx* c);
+cudaError_t launch_step_fp32_tma(ewpt_ctx* c, double Jex, double gam);
+// For the FP32 form, L is the hi/lo buffers' layout (ghost images of hi written).
 int ewpt_launch_bubbles(const Grid& g, double dx, int nb, const double* bubbles, int profile, double p0, double p1,
-                        double p2, double* y, float* hi, float* lo, cudaStream_t st, std::string* err);
+                        double p2, double* y, float* hi, float* lo, const Layout& L, cudaStream_t st,
+                        std::string* err);

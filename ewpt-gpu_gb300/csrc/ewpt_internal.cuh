@@ -15,6 +15,34 @@ struct Grid {
     int64_t S;  // nx*ny*nz
 };
 
+// Storage of one FP32-form [36][.] array set: element (i, j, k) of array a
+// at a*P + o0 + i + px*(j + py*k).  Plain layout (ensemble members): px = nx,
+// py = ny, P = S, o0 = 0.  Ghosted layout (single-lattice FP32 form): every
+// array is a padded box of px x (ny+6) x (nz+6) cells, the sites at x offset
+// 4 and y, z offsets 3, the row pitch px a multiple of 32 floats (128 bytes)
+// with at least 4 spare cells on each x face; the boxes start `lead` = 28
+// floats into the buffer so that every row's first site sits on a 128-byte
+// boundary.  The ghost cells hold the periodic images of the sites within
+// reach of the opposite face (x: 4 cells, y and z: 3); launch_ghost_fill
+// refreshes them after every kernel that writes a stencil source (stage
+// inputs, the state high part), so a stencil reads its neighbours with no
+// wrap and a tile together with its 3-site halo is one dense box (one TMA
+// copy).  A buffer holds 36*P + 32 floats.
+struct Layout {
+    int px, py, pz;
+    int gx, gyz;  // ghost widths: (4, 3) ghosted, (0, 0) plain
+    int64_t P, o0;
+    int lead;     // floats before array 0's padded box
+    __host__ __device__ __forceinline__ int64_t at(int i, int j, int k) const {
+        return o0 + i + (int64_t)px * (j + (int64_t)py * k);
+    }
+};
+inline Layout plain_layout(const Grid& g) { return Layout{g.nx, g.ny, g.nz, 0, 0, g.S, 0, 0}; }
+inline Layout ghost_layout(const Grid& g) {
+    const int px = (g.nx + 8 + 31) / 32 * 32, py = g.ny + 6, pz = g.nz + 6, lead = 28;
+    return Layout{px, py, pz, 4, 3, (int64_t)px * py * pz, lead + 4 + (int64_t)px * (3 + (int64_t)py * 3), lead};
+}
+
 // Stencil coefficients, pre-divided by (60 dx) and dx^2:
 //   d/dx f   = a1 (f1 - f-1) + a2 (f2 - f-2) + a3 (f3 - f-3)
 //   lap f    = l0 f0 + l1 sum(f+-1) + l2 sum(f+-2) + l3 sum(f+-3)
@@ -101,9 +129,13 @@ int tiling_max_threads(int reg);
 
 cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
-cudaError_t launch_step_fp32(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
-                             double Jex, double gam, cudaStream_t st);
-cudaError_t launch_step_fp32_pair(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
-                                  double Jex, double gam, cudaStream_t st);
-cudaError_t launch_fp32_split(const Grid& g, const double* src, Fp32State dst, cudaStream_t st);
-cudaError_t launch_fp32_join(const Grid& g, Fp32State src, double* dst, cudaStream_t st);
+cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
+                             const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+cudaError_t launch_step_fp32_pair(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
+                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+// Copy the face sites of all 36 arrays of a ghosted buffer into their
+// periodic images (stage.cu).
+cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st);
+// FP64 [36][S] <-> FP32 hi/lo in layout L (the ghost images of hi refreshed on split).
+cudaError_t launch_fp32_split(const Grid& g, const Layout& L, const double* src, Fp32State dst, cudaStream_t st);
+cudaError_t launch_fp32_join(const Grid& g, const Layout& L, Fp32State src, double* dst, cudaStream_t st);

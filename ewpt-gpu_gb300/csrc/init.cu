@@ -77,11 +77,14 @@ struct OutF64 {
 struct OutHiLo {
     float* hi;
     float* lo;
-    int64_t S;
+    Grid g;
+    Layout L;
     __device__ void operator()(int a, int64_t c, double v) const {
+        const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((int64_t)g.nx * g.ny));
+        const int64_t q = a * L.P + L.at(i, j, k);
         const float h = (float)v;
-        hi[a * S + c] = h;
-        lo[a * S + c] = (float)(v - (double)h);
+        hi[q] = h;
+        lo[q] = (float)(v - (double)h);
     }
 };
 
@@ -90,7 +93,8 @@ struct OutHiLo {
 // Launch the bubble kernel on a state given as FP64 [36][S] (y != null) or
 // as FP32 hi/lo [36][S] pairs.  bubbles: nb x 7 doubles (centre, direction).
 int ewpt_launch_bubbles(const Grid& g, double dx, int nb, const double* bubbles, int profile, double p0, double p1,
-                        double p2, double* y, float* hi, float* lo, cudaStream_t st, std::string* err) {
+                        double p2, double* y, float* hi, float* lo, const Layout& L, cudaStream_t st,
+                        std::string* err) {
     Bubble* d = nullptr;
     cudaError_t e = cudaMallocAsync(&d, sizeof(Bubble) * (nb > 0 ? nb : 1), st);
     if (e == cudaSuccess && nb > 0) e = cudaMemcpyAsync(d, bubbles, sizeof(Bubble) * nb, cudaMemcpyHostToDevice, st);
@@ -98,8 +102,9 @@ int ewpt_launch_bubbles(const Grid& g, double dx, int nb, const double* bubbles,
         if (y)
             k_bubbles<<<1216, 256, 0, st>>>(g.nx, g.ny, g.nz, dx, d, nb, profile, p0, p1, p2, OutF64{y, g.S});
         else
-            k_bubbles<<<1216, 256, 0, st>>>(g.nx, g.ny, g.nz, dx, d, nb, profile, p0, p1, p2, OutHiLo{hi, lo, g.S});
+            k_bubbles<<<1216, 256, 0, st>>>(g.nx, g.ny, g.nz, dx, d, nb, profile, p0, p1, p2, OutHiLo{hi, lo, g, L});
         e = cudaGetLastError();
+        if (e == cudaSuccess && !y) e = launch_ghost_fill(g, L, hi, st);
     }
     if (d) cudaFreeAsync(d, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -129,9 +134,9 @@ extern "C" int ewpt_init_bubbles(ewpt_ctx* c, int32_t nb, const double* bubbles,
     std::string err;
     rc = c->p.precision == EWPT_FP64
              ? ewpt_launch_bubbles(c->g, c->p.dx, nb, bubbles, profile, q0, p1, c->p.vev, c->y, nullptr, nullptr,
-                                   c->st, &err)
+                                   c->lay, c->st, &err)
              : ewpt_launch_bubbles(c->g, c->p.dx, nb, bubbles, profile, q0, p1, c->p.vev, nullptr, c->y32.hi,
-                                   c->y32.lo, c->st, &err);
+                                   c->y32.lo, c->lay, c->st, &err);
     if (rc) return ewpt_fail(c, rc, "init_bubbles: %s", err.c_str());
     c->it = 0;
     return EWPT_OK;

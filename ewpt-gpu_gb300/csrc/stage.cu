@@ -18,6 +18,8 @@
 //   stage 2, 3:  kacc += 2 k_s;       X3 = y_hi + k2 dt/2,  X4 = y_hi + k3 dt
 //   stage 4:     (y_hi, y_lo) += dt/6 (kacc + k4), compensated, in place
 // (X_1 is y_hi itself).  Bytes per site-update: FP64 4608, FP32 2736.
+#include <algorithm>
+
 #include "accessors.cuh"
 
 namespace {
@@ -106,21 +108,25 @@ __global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMin
 }
 
 // ------------------------------------------------------------- FP32 stage
+// All five FP32 buffers use the ghosted layout L.  After each stage the
+// ghost images of what it wrote (the next stage input, or the state high
+// part after stage 4) are refreshed by k_ghost_fill, so every stencil reads
+// its neighbours with no wrap.
 struct Fp32Bufs {
-    float* yhi;  // [36][S] state, high part (also the stage-1 stencil input)
-    float* ylo;  // [36][S] state, low part
-    float* kacc; // [36][S] RK4-weighted rate sum: k1, then k1 + 2 k2, then k1 + 2 k2 + 2 k3
+    float* yhi;  // [36][P] state, high part (also the stage-1 stencil input)
+    float* ylo;  // [36][P] state, low part
+    float* kacc; // [36][P] RK4-weighted rate sum: k1, then k1 + 2 k2, then k1 + 2 k2 + 2 k3
 };
 
 template <int STAGE>
 struct Fp32Sink {
     const GlobalAcc<float, float>& A;
+    const Layout& L;
     Fp32Bufs b;
     float* __restrict__ xn;
-    int64_t S;
     float h, w6;
     __device__ __forceinline__ void operator()(int a, float r) const {
-        const int64_t q = a * S + A.c;
+        const int64_t q = a * L.P + A.c;
         if (STAGE == 1) {
             b.kacc[q] = r;
             xn[q] = A.v(a) + h * r;  // X1 == y_hi
@@ -140,28 +146,85 @@ struct Fp32Sink {
 };
 
 template <int STAGE, bool BETA, int REG>
-__global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks) k_stage_fp32(Grid g, const __grid_constant__ Ptr36 X, Fp32Bufs b,
-                                                       float* __restrict__ xn, PhysCoef<float> pc,
-                                                       StencilCoef<float> sc, float h, float w6) {
+__global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks)
+    k_stage_fp32(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X, Fp32Bufs b, float* __restrict__ xn,
+                 PhysCoef<float> pc, StencilCoef<float> sc, float h, float w6) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
     GlobalAcc<float, float> A{{X}};
-    if (!make_acc(g, sc, A)) return;
-    Fp32Sink<STAGE> out{A, b, xn, g.S, h, w6};
+    A.place_ghost(i, j, k, L);
+    A.s = sc;
+    Fp32Sink<STAGE> out{A, L, b, xn, h, w6};
     site_rates<float, BETA>(A, pc, out);
 }
 
-__global__ void k_split(int64_t n, const double* __restrict__ src, float* __restrict__ hi, float* __restrict__ lo) {
+// FP64 [36][S] -> (hi, lo) in layout L (ghost cells left to k_ghost_fill).
+__global__ void k_split(Grid g, Layout L, const double* __restrict__ src, float* __restrict__ hi,
+                        float* __restrict__ lo) {
+    const int64_t n = 36 * g.S;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / g.S);
+        const int64_t c = q - a * g.S;
+        const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((int64_t)g.nx * g.ny));
         const double v = src[q];
         const float h = (float)v;
-        hi[q] = h;
-        lo[q] = (float)(v - (double)h);
+        const int64_t d = a * L.P + L.at(i, j, k);
+        hi[d] = h;
+        lo[d] = (float)(v - (double)h);
     }
 }
 
-__global__ void k_join(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+__global__ void k_join(Grid g, Layout L, const float* __restrict__ hi, const float* __restrict__ lo,
                        double* __restrict__ dst) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        dst[q] = (double)hi[q] + (double)lo[q];
+    const int64_t n = 36 * g.S;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / g.S);
+        const int64_t c = q - a * g.S;
+        const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((int64_t)g.nx * g.ny));
+        const int64_t d = a * L.P + L.at(i, j, k);
+        dst[q] = (double)hi[d] + (double)lo[d];
+    }
+}
+
+// Ghost images of a ghosted buffer: one thread per ghost cell of array
+// blockIdx.y, over three segments -- the x faces (4 + 4 cells per row), the y
+// faces (3 + 3 rows per plane) and the z faces (3 + 3 planes); each copies the
+// site it is the periodic image of.  The box edges and corners are left
+// alone (no axis-aligned stencil reaches them).  32-bit index arithmetic (a
+// segment of one array has fewer than 2^31 cells).
+__global__ void k_ghost_fill(Grid g, Layout L, float* __restrict__ buf) {
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int nxs = 8 * ny * nz, nys = 6 * nx * nz, nzs = 6 * nx * ny, per = nxs + nys + nzs;
+    float* arr = buf + blockIdx.y * L.P;
+    for (int e0 = blockIdx.x * blockDim.x + threadIdx.x; e0 < per; e0 += gridDim.x * blockDim.x) {
+        int e = e0, di, dj, dk, si, sj, sk;
+        if (e < nxs) {
+            const int xg = e & 7;
+            e >>= 3;
+            dj = sj = e % ny;
+            dk = sk = e / ny;
+            di = xg < 4 ? xg - 4 : nx + xg - 4;
+            si = xg < 4 ? nx + xg - 4 : xg - 4;
+        } else if ((e -= nxs) < nys) {
+            di = si = e % nx;
+            e /= nx;
+            const int yg = e % 6;
+            dk = sk = e / 6;
+            dj = yg < 3 ? yg - 3 : ny + yg - 3;
+            sj = yg < 3 ? ny + yg - 3 : yg - 3;
+        } else {
+            e -= nys;
+            di = si = e % nx;
+            e /= nx;
+            dj = sj = e % ny;
+            const int zg = e / ny;
+            dk = zg < 3 ? zg - 3 : nz + zg - 3;
+            sk = zg < 3 ? nz + zg - 3 : zg - 3;
+        }
+        arr[L.at(di, dj, dk)] = arr[L.at(si, sj, sk)];
+    }
 }
 
 inline dim3 grid_of(const Grid& g, const Tiling& t) {
@@ -224,45 +287,58 @@ cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* 
 
 // FP32 form: stage inputs ping-pong between xa and xb.
 template <bool BETA, int REG>
-static void step_fp32(const Grid& g, const Tiling& t, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
-                      const StencilCoef<float>& sc, double dt, cudaStream_t st) {
+static void step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32Bufs b, float* xa, float* xb,
+                      const PhysCoef<float>& pc, const StencilCoef<float>& sc, double dt, cudaStream_t st) {
     const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
     const float h2 = (float)(dt / 2.), h1 = (float)dt, w6 = (float)(dt / 6.);
-    k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack(b.yhi, g.S, 4), b, xa, pc, sc, h2, w6);
-    k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, xb, pc, sc, h2, w6);
-    k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 4), b, xa, pc, sc, h1, w6);
-    k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 4), b, nullptr, pc, sc, 0.f, w6);
+    k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(b.yhi, L.P, 4), b, xa, pc, sc, h2, w6);
+    launch_ghost_fill(g, L, xa, st);
+    k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, xb, pc, sc, h2, w6);
+    launch_ghost_fill(g, L, xb, st);
+    k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xb, L.P, 4), b, xa, pc, sc, h1, w6);
+    launch_ghost_fill(g, L, xa, st);
+    k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, nullptr, pc, sc, 0.f, w6);
+    launch_ghost_fill(g, L, b.yhi, st);
 }
 
 template <bool BETA>
-static void step_fp32_r(const Grid& g, const Tiling& t, Fp32Bufs b, float* xa, float* xb, const PhysCoef<float>& pc,
-                        const StencilCoef<float>& sc, double dt, cudaStream_t st) {
+static void step_fp32_r(const Grid& g, const Layout& L, const Tiling& t, Fp32Bufs b, float* xa, float* xb,
+                        const PhysCoef<float>& pc, const StencilCoef<float>& sc, double dt, cudaStream_t st) {
     if (t.reg == 1)
-        step_fp32<BETA, 1>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_fp32<BETA, 1>(g, L, t, b, xa, xb, pc, sc, dt, st);
     else if (t.reg == 2)
-        step_fp32<BETA, 2>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_fp32<BETA, 2>(g, L, t, b, xa, xb, pc, sc, dt, st);
     else
-        step_fp32<BETA, 0>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_fp32<BETA, 0>(g, L, t, b, xa, xb, pc, sc, dt, st);
 }
 
-cudaError_t launch_step_fp32(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
-                             double Jex, double gam, cudaStream_t st) {
+cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
+                             const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+    if (L.gx == 0) return cudaErrorInvalidValue;  // the single-lattice kernels read ghost cells
     const PhysCoef<float> pc = make_phys<float>(p, Jex, gam);
     const StencilCoef<float> sc = make_stencil<float>(p.dx);
     Fp32Bufs b{y.hi, y.lo, w.kacc};
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_fp32_r<true>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_fp32_r<true>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     else
-        step_fp32_r<false>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_fp32_r<false>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fp32_split(const Grid& g, const double* src, Fp32State dst, cudaStream_t st) {
-    k_split<<<1216, 256, 0, st>>>(36 * g.S, src, dst.hi, dst.lo);
+cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st) {
+    if (L.gx == 0) return cudaSuccess;
+    const int64_t per = 8LL * g.ny * g.nz + 6LL * g.nx * g.nz + 6LL * g.nx * g.ny;
+    const int bx = (int)std::min<int64_t>((per + 255) / 256, 64);
+    k_ghost_fill<<<dim3(bx, 36), 256, 0, st>>>(g, L, buf);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fp32_join(const Grid& g, Fp32State src, double* dst, cudaStream_t st) {
-    k_join<<<1216, 256, 0, st>>>(36 * g.S, src.hi, src.lo, dst);
+cudaError_t launch_fp32_split(const Grid& g, const Layout& L, const double* src, Fp32State dst, cudaStream_t st) {
+    k_split<<<1216, 256, 0, st>>>(g, L, src, dst.hi, dst.lo);
+    return launch_ghost_fill(g, L, dst.hi, st);
+}
+
+cudaError_t launch_fp32_join(const Grid& g, const Layout& L, Fp32State src, double* dst, cudaStream_t st) {
+    k_join<<<1216, 256, 0, st>>>(g, L, src.hi, src.lo, dst);
     return cudaGetLastError();
 }

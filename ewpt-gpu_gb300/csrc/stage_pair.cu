@@ -6,8 +6,10 @@
 // FADD2 / FMUL2 for both sites, and every neighbour access is a float2 load.
 // For the x stencil the pairs at i0-4, i0-2, i0, i0+2, i0+4 (five aligned
 // float2 loads) are re-paired into the +-1, +-2, +-3 neighbour pairs; y and z
-// neighbours are aligned float2 loads of the same x pair.  Needs nx even
-// (a pair never straddles the periodic wrap).
+// neighbours are aligned float2 loads of the same x pair.  The buffers use
+// the ghosted layout (ewpt_internal.cuh), so neighbours past a face are read
+// from the ghost cells, refreshed by k_ghost_fill after each stage.  Needs
+// nx even.
 #include "accessors.cuh"
 
 namespace {
@@ -30,16 +32,16 @@ struct PairBufs {
 template <int STAGE>
 struct PairSink {
     const PairAcc<SrcPtr36<float>>& A;
+    const Layout& L;
     PairBufs b;
     float* __restrict__ xn;
-    int64_t S;
     f2 h, w6;
     __device__ __forceinline__ static float2* at(float* base, int64_t q) { return reinterpret_cast<float2*>(base + q); }
     __device__ __forceinline__ static float2 rd(const float* base, int64_t q) {
         return __ldg(reinterpret_cast<const float2*>(base + q));
     }
     __device__ __forceinline__ void operator()(int a, f2 r) const {
-        const int64_t q = a * S + A.c;
+        const int64_t q = a * L.P + A.c;
         if (STAGE == 1) {
             *at(b.kacc, q) = r.v;
             *at(xn, q) = (A.v(a) + h * r).v;
@@ -59,7 +61,7 @@ struct PairSink {
 
 template <int STAGE, bool BETA, int REG>
 __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kMinBlocks)
-    k_stage_fp32x2(Grid g, const __grid_constant__ Ptr36 X, PairBufs b, float* __restrict__ xn,
+    k_stage_fp32x2(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X, PairBufs b, float* __restrict__ xn,
                    PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6) {
     const int ip = blockIdx.x * blockDim.x + threadIdx.x;  // pair index along x
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -67,9 +69,9 @@ __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kM
     const int i0 = 2 * ip;
     if (i0 >= g.nx || j >= g.ny) return;
     PairAcc<SrcPtr36<float>> A{{X}};
-    A.place(i0, j, k, g.nx, g.ny, g.nz);
+    A.place_ghost(i0, j, k, L);
     A.s = sc;
-    PairSink<STAGE> out{A, b, xn, g.S, h, w6};
+    PairSink<STAGE> out{A, L, b, xn, h, w6};
     site_rates<f2, BETA>(A, pc, out);
 }
 
@@ -80,39 +82,43 @@ Ptr36 pack4(const void* base, int64_t S) {
 }
 
 template <bool BETA, int REG>
-void step_pair(const Grid& g, const Tiling& t, PairBufs b, float* xa, float* xb, const PhysCoef<f2>& pc,
-               const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
+void step_pair(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, float* xa, float* xb,
+               const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
     const int npx = g.nx / 2;
     const dim3 gr((npx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz), bl(t.bx, t.by);
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
-    k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack4(b.yhi, g.S), b, xa, pc, sc, h2, w6);
-    k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack4(xa, g.S), b, xb, pc, sc, h2, w6);
-    k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack4(xb, g.S), b, xa, pc, sc, h1, w6);
-    k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack4(xa, g.S), b, nullptr, pc, sc, z, w6);
+    k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6);
+    launch_ghost_fill(g, L, xa, st);
+    k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6);
+    launch_ghost_fill(g, L, xb, st);
+    k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6);
+    launch_ghost_fill(g, L, xa, st);
+    k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6);
+    launch_ghost_fill(g, L, b.yhi, st);
 }
 
 template <bool BETA>
-void step_pair_r(const Grid& g, const Tiling& t, PairBufs b, float* xa, float* xb, const PhysCoef<f2>& pc,
-                 const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
+void step_pair_r(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, float* xa, float* xb,
+                 const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
     if (t.reg == 1)
-        step_pair<BETA, 1>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_pair<BETA, 1>(g, L, t, b, xa, xb, pc, sc, dt, st);
     else if (t.reg == 2)
-        step_pair<BETA, 2>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_pair<BETA, 2>(g, L, t, b, xa, xb, pc, sc, dt, st);
     else
-        step_pair<BETA, 0>(g, t, b, xa, xb, pc, sc, dt, st);
+        step_pair<BETA, 0>(g, L, t, b, xa, xb, pc, sc, dt, st);
 }
 
 }  // namespace
 
-cudaError_t launch_step_fp32_pair(const Grid& g, const Tiling& t, Fp32State y, Fp32Work w, const ewpt_params& p,
-                                  double Jex, double gam, cudaStream_t st) {
-    if (g.nx % 2 != 0) return cudaErrorInvalidValue;
+cudaError_t launch_step_fp32_pair(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
+                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+    if (g.nx % 2 != 0 || L.gx == 0) return cudaErrorInvalidValue;
     const PhysCoef<f2> pc = make_phys<f2>(p, Jex, gam);
     const StencilCoef<f2> sc = pair_stencil(make_stencil<float>(p.dx));
     PairBufs b{y.hi, y.lo, w.kacc};
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_pair_r<true>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_pair_r<true>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     else
-        step_pair_r<false>(g, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_pair_r<false>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
     return cudaGetLastError();
 }

@@ -22,6 +22,8 @@ CANDIDATES = [(32, 4, 0, 0), (64, 2, 0, 0), (32, 2, 0, 0), (16, 8, 0, 0), (128, 
 # FP32 form only: two sites per thread (needs even nx)
 PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (32, 1, 0, 1),
                    (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1)]
+# FP32 form only: TMA-staged tiles of 32 x by x bz sites, (bx, by, bz, 2)
+TMA_CANDIDATES = [(32, 4, 4, 2), (32, 2, 4, 2)]
 
 
 def cache_path() -> str:
@@ -78,6 +80,9 @@ def sweep(p: Params, steps: int = 2, candidates=None) -> list:
         candidates = list(CANDIDATES)
         if int(p.precision) == _lib.FP32 and p.dims[0] % 2 == 0:
             candidates += PAIR_CANDIDATES
+        nx, ny, nz = p.dims
+        if int(p.precision) == _lib.FP32 and nx % 32 == 0:
+            candidates += [t for t in TMA_CANDIDATES if ny % t[1] == 0 and nz % t[2] == 0]
     res = []
     with Lattice(p) as lat:
         lat.set_state(ic.bubbles_tanh(p.dims, p.dx, 4, seed=0))

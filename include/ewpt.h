@@ -101,13 +101,17 @@ int ewpt_step(ewpt_ctx* ctx, int32_t nsteps);
 int ewpt_step_explicit(ewpt_ctx* ctx, int32_t nsteps, double Jex, double gamma);
 /* Iterations done so far (the `it` of the reference loop). */
 int64_t ewpt_iteration(const ewpt_ctx* ctx);
-/* Launch shape of the stage kernels: blocks of bx*by threads over x and y
- * (whole warps, at most 128 threads), reg = register-budget variant (0:
- * registers at the compiler's choice; 1: <= 128 registers; 2: <= 168);
- * pair = 1 (FP32 form, even nx): each thread evolves two x-adjacent sites
- * with packed FP32x2 arithmetic.  The result of a step does not depend on
- * bx, by or reg, and pair only changes FP32 rounding; ewpt/autotune.py
- * picks the fastest per lattice size and precision.  Default 32x4, 0, 0. */
+/* Launch shape of the stage kernels.  pair = 0 or 1: blocks of bx*by
+ * threads over x and y (whole warps, at most 128 threads), reg = register-
+ * budget variant (0: registers at the compiler's choice; 1: <= 128
+ * registers; 2: <= 168); pair = 1 (FP32 form, even nx): each thread evolves
+ * two x-adjacent sites with packed FP32x2 arithmetic.  pair = 2 (FP32 form):
+ * TMA-staged shared-memory tiles of bx x by x reg sites -- bx = 32, by = 4 or
+ * 2, reg = 4 (the tile's z extent); needs nx % 32 == 0, ny % by == 0,
+ * nz % 4 == 0 -- with the same arithmetic as pair = 1.  The result of a step
+ * does not depend on bx, by or reg, and pair only changes FP32 rounding
+ * (pair = 1 and 2 agree bit for bit); ewpt/autotune.py picks the fastest per
+ * lattice size and precision.  Default 32x4, 0, 0. */
 int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg, int32_t pair);
 int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair);
 /* Wait for all work queued on the context. */

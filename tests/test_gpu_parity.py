@@ -194,6 +194,66 @@ def test_fp32_tilings_agree(tile):
     assert rel_err(res[1], res[0]) < 2e-5
 
 
+@pytest.mark.parametrize("shape,beta", [((32, 24, 20), 0.2), ((64, 8, 12), 0.0), ((32, 8, 8), 0.1)])
+def test_fp32_tma_tiles_match_pair_kernel(shape, beta):
+    """TMA-staged shared-memory tiles (tiling mode 2) run the same packed
+    FP32x2 arithmetic as the two-sites-per-thread kernel: bit-identical
+    states, through the J_ext/damp schedule and with beta terms, on lattices
+    with one to eight tiles per axis, so boxes at every face read their halo
+    from the ghost cells."""
+    p32 = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, precision=ewpt.FP32, beta_w=beta,
+                                  beta_y=0.5 * beta)
+    y0 = perturbed_bubbles(shape, p32.dx, 3, seed=11, amp=0.02)
+    res = []
+    for t in [(32, 4, 0, 1), (32, 4, 4, 2), (32, 2, 4, 2)]:
+        with ewpt.Lattice(p32) as lat:
+            lat.set_state(y0)
+            lat.set_tiling(*t)
+            assert lat.tiling() == t
+            lat.step(6, Jex=0.03, gamma=0.01)
+            lat.step(6)
+            res.append(lat.get_state())
+            d = lat.diagnostics()
+    for r in res[1:]:
+        np.testing.assert_array_equal(r, res[0])
+    assert np.isfinite(d).all()
+
+
+def test_fp32_tma_tiles_switch_modes_midrun():
+    """The three FP32 tiling modes share one state: switching mid-run gives
+    the same evolution as staying in the paired mode."""
+    shape = (32, 16, 16)
+    p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32)
+    y0 = perturbed_bubbles(shape, p32.dx, 2, seed=5, amp=0.02)
+    with ewpt.Lattice(p32) as lat:
+        lat.set_state(y0)
+        lat.set_tiling(32, 4, 0, 1)
+        lat.step(9)
+        ref = lat.get_state()
+    with ewpt.Lattice(p32) as lat:
+        lat.set_state(y0)
+        for t in ((32, 4, 4, 2), (32, 4, 0, 1), (32, 2, 4, 2)):
+            lat.set_tiling(*t)
+            lat.step(3)
+        got = lat.get_state()
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_fp32_tma_tiles_reject_bad_contexts():
+    p64 = ewpt.baseline_couplings(shape=(32, 8, 8), N=32, dx=0.25, dt=0.025)
+    with ewpt.Lattice(p64) as lat, pytest.raises(ewpt.EwptError):
+        lat.set_tiling(32, 4, 4, 2)  # FP64 context
+    p32 = ewpt.baseline_couplings(shape=(24, 8, 8), N=24, dx=0.25, dt=0.025, precision=ewpt.FP32)
+    with ewpt.Lattice(p32) as lat:
+        with pytest.raises(ewpt.EwptError):
+            lat.set_tiling(32, 4, 4, 2)  # nx not a multiple of 32
+        with pytest.raises(ewpt.EwptError):
+            lat.set_tiling(32, 3, 4, 2)  # tile shape not offered
+        with pytest.raises(ewpt.EwptError):
+            lat.set_tiling(32, 4, 2, 2)
+        assert lat.tiling() == (32, 4, 0, 0)
+
+
 def test_fp32_form_tracks_fp64():
     """FP32 form vs FP64 on a smooth bubble IC: fields within 1e-4 of FP64
     after 100 steps, energy drift and Gauss violation within 2x of FP64
@@ -203,11 +263,13 @@ def test_fp32_form_tracks_fp64():
     p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32)
     y0 = ewpt.ic.bubbles_tanh(shape, p64.dx, 4, seed=21)
     res = {}
-    for name, p in (("64", p64), ("32", p32), ("32x2", p32)):
+    for name, p in (("64", p64), ("32", p32), ("32x2", p32), ("32tma", p32)):
         with ewpt.Lattice(p) as lat:
             lat.set_state(y0)
             if name == "32x2":
                 lat.set_tiling(32, 4, 0, 1)
+            if name == "32tma":
+                lat.set_tiling(32, 4, 4, 2)
             d0 = lat.diagnostics()
             lat.step(100)
             res[name] = (lat.get_state(), d0, lat.diagnostics(), lat.spectrum("B", "log", 12))
@@ -217,7 +279,7 @@ def test_fp32_form_tracks_fp64():
     g64 = res["64"][2][14]
     s64 = res["64"][3]["mean"]
     m = s64 > 1e-12 * s64.max()
-    for name in ("32", "32x2"):
+    for name in ("32", "32x2", "32tma"):
         y32 = res[name][0]
         assert rel_err(y32[:20], y64[:20]) < 1e-4
         drift32 = abs(res[name][2][13] - e0)

@@ -79,14 +79,15 @@ struct SiteAcc {
         axis_offsets(j, ny, nx, oy);
         axis_offsets(k, nz, nx * ny, oz);
     }
-    // site (i, j, k) of a ghosted layout: the neighbours are plain strides
-    __device__ __forceinline__ void place_ghost(int i, int j, int k, const Layout& L) {
+    // site (i, j, k) of a ghosted layout: y and z neighbours are plain
+    // strides (ghost cells), x neighbours wrap (the x ghost cells are kept
+    // only for the TMA-staged kernel)
+    __device__ __forceinline__ void place_ghost(int i, int j, int k, int nx, const Layout& L) {
         c = (int)L.at(i, j, k);
         const int sy = L.px, sz = L.px * L.py;
+        axis_offsets(i, nx, 1, ox);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            ox[d] = d + 1;
-            ox[d + 3] = -(d + 1);
             oy[d] = (d + 1) * sy;
             oy[d + 3] = -(d + 1) * sy;
             oz[d] = (d + 1) * sz;
@@ -171,14 +172,14 @@ struct PairAcc {
         axis_offsets(j, ny, nx, oy);
         axis_offsets(k, nz, nx * ny, oz);
     }
-    // pair (i0, i0+1) of a ghosted layout
-    __device__ __forceinline__ void place_ghost(int i0, int j, int k, const Layout& L) {
+    // pair (i0, i0+1) of a ghosted layout (y, z from ghost cells, x wrapped)
+    __device__ __forceinline__ void place_ghost(int i0, int j, int k, int nx, const Layout& L) {
         c = (int)L.at(i0, j, k);
         const int sy = L.px, sz = L.px * L.py;
-        ox[0] = -4;
-        ox[1] = -2;
-        ox[2] = 2;
-        ox[3] = 4;
+        ox[0] = (i0 - 4 >= 0 ? -4 : nx - 4);
+        ox[1] = (i0 - 2 >= 0 ? -2 : nx - 2);
+        ox[2] = (i0 + 2 < nx ? 2 : 2 - nx);
+        ox[3] = (i0 + 4 < nx ? 4 : 4 - nx);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             oy[d] = (d + 1) * sy;

@@ -294,6 +294,9 @@ int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pa
         if (c->p.precision != EWPT_FP32) return ewpt_fail(c, EWPT_ERR_ARG, "TMA tiles need the FP32 form");
         int rc = ewpt_tma_prepare(c, by, reg);
         if (rc) return rc;
+        // the other FP32 kernels leave the x ghost cells stale; the TMA boxes read them
+        rc = ewpt_cuda_check(c, launch_ghost_fill(c->g, c->lay, c->y32.hi, c->st, true), "ghost fill");
+        if (rc) return rc;
         c->tile = Tiling{bx, by, reg, pair};
         return EWPT_OK;
     }

@@ -134,8 +134,8 @@ cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp
 cudaError_t launch_step_fp32_pair(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
                                   const ewpt_params& p, double Jex, double gam, cudaStream_t st);
 // Copy the face sites of all 36 arrays of a ghosted buffer into their
-// periodic images (stage.cu).
-cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st);
+// periodic images (stage.cu); the x faces only if xfaces.
+cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st, bool xfaces);
 // FP64 [36][S] <-> FP32 hi/lo in layout L (the ghost images of hi refreshed on split).
 cudaError_t launch_fp32_split(const Grid& g, const Layout& L, const double* src, Fp32State dst, cudaStream_t st);
 cudaError_t launch_fp32_join(const Grid& g, const Layout& L, Fp32State src, double* dst, cudaStream_t st);

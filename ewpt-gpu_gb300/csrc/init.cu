@@ -104,7 +104,7 @@ int ewpt_launch_bubbles(const Grid& g, double dx, int nb, const double* bubbles,
         else
             k_bubbles<<<1216, 256, 0, st>>>(g.nx, g.ny, g.nz, dx, d, nb, profile, p0, p1, p2, OutHiLo{hi, lo, g, L});
         e = cudaGetLastError();
-        if (e == cudaSuccess && !y) e = launch_ghost_fill(g, L, hi, st);
+        if (e == cudaSuccess && !y) e = launch_ghost_fill(g, L, hi, st, true);
     }
     if (d) cudaFreeAsync(d, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

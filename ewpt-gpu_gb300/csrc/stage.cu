@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMin
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return;
     GlobalAcc<float, float> A{{X}};
-    A.place_ghost(i, j, k, L);
+    A.place_ghost(i, j, k, g.nx, L);
     A.s = sc;
     Fp32Sink<STAGE> out{A, L, b, xn, h, w6};
     site_rates<float, BETA>(A, pc, out);
@@ -188,42 +188,48 @@ __global__ void k_join(Grid g, Layout L, const float* __restrict__ hi, const flo
     }
 }
 
-// Ghost images of a ghosted buffer: one thread per ghost cell of array
-// blockIdx.y, over three segments -- the x faces (4 + 4 cells per row), the y
-// faces (3 + 3 rows per plane) and the z faces (3 + 3 planes); each copies the
-// site it is the periodic image of.  The box edges and corners are left
-// alone (no axis-aligned stencil reaches them).  32-bit index arithmetic (a
-// segment of one array has fewer than 2^31 cells).
-__global__ void k_ghost_fill(Grid g, Layout L, float* __restrict__ buf) {
+// Ghost images of a ghosted buffer, one warp per work item over a grid of a
+// few blocks per SM: first the y- and z-face rows (a warp copies one row of
+// nx sites into one of the 3 + 3 ghost rows of an x-y plane, or into a row
+// of one of the 3 + 3 ghost planes), then, if asked, the x faces (a warp
+// serves 4 rows, 8 cells each: the 4 ghost cells before the row and the 4
+// after it).  The x faces cost most of the time (16-byte pieces of every
+// row, 0.86 GB of DRAM reads per launch at 256^3 with them against ~0.12 GB
+// without), so only the TMA-staged kernel, whose boxes read them, keeps
+// them; the other FP32 kernels wrap x in their neighbour offsets.  Every
+// cell copies the site it is the periodic image of; the box edges and
+// corners are left alone (no axis-aligned stencil reaches them).
+__global__ void __launch_bounds__(256) k_ghost_fill(Grid g, Layout L, float* __restrict__ buf, int xfaces) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int nxs = 8 * ny * nz, nys = 6 * nx * nz, nzs = 6 * nx * ny, per = nxs + nys + nzs;
-    float* arr = buf + blockIdx.y * L.P;
-    for (int e0 = blockIdx.x * blockDim.x + threadIdx.x; e0 < per; e0 += gridDim.x * blockDim.x) {
-        int e = e0, di, dj, dk, si, sj, sk;
-        if (e < nxs) {
-            const int xg = e & 7;
-            e >>= 3;
-            dj = sj = e % ny;
-            dk = sk = e / ny;
-            di = xg < 4 ? xg - 4 : nx + xg - 4;
-            si = xg < 4 ? nx + xg - 4 : xg - 4;
-        } else if ((e -= nxs) < nys) {
-            di = si = e % nx;
-            e /= nx;
-            const int yg = e % 6;
-            dk = sk = e / 6;
-            dj = yg < 3 ? yg - 3 : ny + yg - 3;
-            sj = yg < 3 ? ny + yg - 3 : yg - 3;
+    const int px = L.px, pxy = L.px * L.py;
+    const int lane = threadIdx.x & 31;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int per_a = 6 * (ny + nz);
+    for (int r = w0; r < 36 * per_a; r += nw) {
+        const int a = r / per_a, e = r - a * per_a;
+        float* arr = buf + a * L.P + L.o0;  // site (0, 0, 0)
+        int doff, soff;
+        if (e < 6 * nz) {
+            const int yg = e % 6, k = e / 6;
+            doff = (yg < 3 ? yg - 3 : ny + yg - 3) * px + k * pxy;
+            soff = (yg < 3 ? ny + yg - 3 : yg - 3) * px + k * pxy;
         } else {
-            e -= nys;
-            di = si = e % nx;
-            e /= nx;
-            dj = sj = e % ny;
-            const int zg = e / ny;
-            dk = zg < 3 ? zg - 3 : nz + zg - 3;
-            sk = zg < 3 ? nz + zg - 3 : zg - 3;
+            const int zg = (e - 6 * nz) % 6, j = (e - 6 * nz) / 6;
+            doff = j * px + (zg < 3 ? zg - 3 : nz + zg - 3) * pxy;
+            soff = j * px + (zg < 3 ? nz + zg - 3 : zg - 3) * pxy;
         }
-        arr[L.at(di, dj, dk)] = arr[L.at(si, sj, sk)];
+        for (int i = lane; i < nx; i += 32) arr[doff + i] = arr[soff + i];
+    }
+    if (!xfaces) return;
+    const int rows = ny * nz, quads = (36 * rows + 3) / 4;
+    const int xg = lane & 7;
+    const int di = xg < 4 ? xg - 4 : nx + xg - 4, si = xg < 4 ? nx + xg - 4 : xg - 4;
+    for (int q = w0; q < quads; q += nw) {
+        const int rr = 4 * q + (lane >> 3);
+        if (rr >= 36 * rows) continue;
+        const int a = rr / rows, row = rr - a * rows;
+        float* base = buf + a * L.P + L.o0 + (row % ny) * px + (row / ny) * pxy;
+        base[di] = base[si];
     }
 }
 
@@ -292,13 +298,13 @@ static void step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32Bufs 
     const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
     const float h2 = (float)(dt / 2.), h1 = (float)dt, w6 = (float)(dt / 6.);
     k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(b.yhi, L.P, 4), b, xa, pc, sc, h2, w6);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, false);
     k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, xb, pc, sc, h2, w6);
-    launch_ghost_fill(g, L, xb, st);
+    launch_ghost_fill(g, L, xb, st, false);
     k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xb, L.P, 4), b, xa, pc, sc, h1, w6);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, false);
     k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, nullptr, pc, sc, 0.f, w6);
-    launch_ghost_fill(g, L, b.yhi, st);
+    launch_ghost_fill(g, L, b.yhi, st, false);
 }
 
 template <bool BETA>
@@ -325,17 +331,15 @@ cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp
     return cudaGetLastError();
 }
 
-cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st) {
+cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st, bool xfaces) {
     if (L.gx == 0) return cudaSuccess;
-    const int64_t per = 8LL * g.ny * g.nz + 6LL * g.nx * g.nz + 6LL * g.nx * g.ny;
-    const int bx = (int)std::min<int64_t>((per + 255) / 256, 64);
-    k_ghost_fill<<<dim3(bx, 36), 256, 0, st>>>(g, L, buf);
+    k_ghost_fill<<<152 * 8, 256, 0, st>>>(g, L, buf, xfaces ? 1 : 0);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fp32_split(const Grid& g, const Layout& L, const double* src, Fp32State dst, cudaStream_t st) {
     k_split<<<1216, 256, 0, st>>>(g, L, src, dst.hi, dst.lo);
-    return launch_ghost_fill(g, L, dst.hi, st);
+    return launch_ghost_fill(g, L, dst.hi, st, true);
 }
 
 cudaError_t launch_fp32_join(const Grid& g, const Layout& L, Fp32State src, double* dst, cudaStream_t st) {

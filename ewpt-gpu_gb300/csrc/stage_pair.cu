@@ -8,8 +8,8 @@
 // float2 loads) are re-paired into the +-1, +-2, +-3 neighbour pairs; y and z
 // neighbours are aligned float2 loads of the same x pair.  The buffers use
 // the ghosted layout (ewpt_internal.cuh), so neighbours past a face are read
-// from the ghost cells, refreshed by k_ghost_fill after each stage.  Needs
-// nx even.
+// from the ghost cells along y and z (refreshed by k_ghost_fill after each
+// stage) and wrapped in the offsets along x.  Needs nx even.
 #include "accessors.cuh"
 
 namespace {
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kM
     const int i0 = 2 * ip;
     if (i0 >= g.nx || j >= g.ny) return;
     PairAcc<SrcPtr36<float>> A{{X}};
-    A.place_ghost(i0, j, k, L);
+    A.place_ghost(i0, j, k, g.nx, L);
     A.s = sc;
     PairSink<STAGE> out{A, L, b, xn, h, w6};
     site_rates<f2, BETA>(A, pc, out);
@@ -88,13 +88,13 @@ void step_pair(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, floa
     const dim3 gr((npx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz), bl(t.bx, t.by);
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
     k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, false);
     k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6);
-    launch_ghost_fill(g, L, xb, st);
+    launch_ghost_fill(g, L, xb, st, false);
     k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, false);
     k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6);
-    launch_ghost_fill(g, L, b.yhi, st);
+    launch_ghost_fill(g, L, b.yhi, st, false);
 }
 
 template <bool BETA>

@@ -569,13 +569,13 @@ void step_tma(const Grid& g, const Layout& L, const TmaState& T, TmaBufs b, floa
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
     const int G = T.grid, n = C::NTHREADS, sm = C::SMEM_BYTES;
     k_stage_tma<1, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.yhi, T.epi, b.yhi, b, xa, pc, sc, h2, w6, T.err);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, true);
     k_stage_tma<2, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, xb, pc, sc, h2, w6, T.err);
-    launch_ghost_fill(g, L, xb, st);
+    launch_ghost_fill(g, L, xb, st, true);
     k_stage_tma<3, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xb, T.epi, xb, b, xa, pc, sc, h1, w6, T.err);
-    launch_ghost_fill(g, L, xa, st);
+    launch_ghost_fill(g, L, xa, st, true);
     k_stage_tma<4, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, nullptr, pc, sc, z, w6, T.err);
-    launch_ghost_fill(g, L, b.yhi, st);
+    launch_ghost_fill(g, L, b.yhi, st, true);
 }
 
 template <int TBY, int TBZ>

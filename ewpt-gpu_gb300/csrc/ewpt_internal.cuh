@@ -71,6 +71,28 @@ __device__ __forceinline__ void axis_offsets(int i, int n, int stride, int* o) {
     o[5] = (i - 3 >= 0 ? -3 : n - 3) * stride;
 }
 
+// Rows of y per L2 chunk of the FP32 stage kernels' block walk.  A z plane's stencil reads
+// planes k-3..k+3 of all 36 arrays; walking the lattice plane by plane over
+// whole 256^2 planes keeps ~110 MB of inputs live, too close to the 126 MB
+// L2 next to the streaming outputs, and 30% of the stencil loads went back
+// to DRAM (12.8 ms per step at 256^3).  Chunks of 8/16/24/32/64 rows
+// measured 11.96/11.36/11.16/11.09/11.56 ms per step.
+constexpr int kChunkRows = 32;
+
+// Block b of a 1-D grid over nbx x nby blocks per plane and nz planes,
+// walked x fastest, then the block rows of one y chunk of ycb block rows,
+// then z, then the chunks: one chunk's 7-plane working set of all 36 arrays
+// stays in L2 while the chunk sweeps z.
+__device__ __forceinline__ void chunk_walk(int b, int nbx, int nby, int nz, int ycb, int& bx, int& by, int& k) {
+    bx = b % nbx;
+    b /= nbx;
+    const int c = b / (ycb * nz), rem = b - c * ycb * nz;
+    const int yc = min(ycb, nby - c * ycb);
+    by = c * ycb + rem % yc;
+    k = rem / yc;
+}
+
+
 template <typename T>
 PhysCoef<T> make_phys(const ewpt_params& p, double Jex, double gam) {
     PhysCoef<T> c;

@@ -147,11 +147,13 @@ struct Fp32Sink {
 
 template <int STAGE, bool BETA, int REG>
 __global__ void __launch_bounds__(RegBudget<REG>::kThreads, RegBudget<REG>::kMinBlocks)
-    k_stage_fp32(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X, Fp32Bufs b, float* __restrict__ xn,
-                 PhysCoef<float> pc, StencilCoef<float> sc, float h, float w6) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+    k_stage_fp32(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X,
+                 Fp32Bufs b, float* __restrict__ xn, PhysCoef<float> pc, StencilCoef<float> sc, float h, float w6,
+                 int nbx, int nby, int ycb) {
+    int bx, by, k;
+    chunk_walk(blockIdx.x, nbx, nby, g.nz, ycb, bx, by, k);
+    const int i = bx * blockDim.x + threadIdx.x;
+    const int j = by * blockDim.y + threadIdx.y;
     if (i >= g.nx || j >= g.ny) return;
     GlobalAcc<float, float> A{{X}};
     A.place_ghost(i, j, k, g.nx, L);
@@ -295,16 +297,20 @@ cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* 
 template <bool BETA, int REG>
 static void step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32Bufs b, float* xa, float* xb,
                       const PhysCoef<float>& pc, const StencilCoef<float>& sc, double dt, cudaStream_t st) {
-    const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
+    const int nbx = (g.nx + t.bx - 1) / t.bx, nby = (g.ny + t.by - 1) / t.by;
+    const int ycb = std::max(1, kChunkRows / t.by);
+    const dim3 gr(nbx * nby * g.nz), bl(t.bx, t.by);
     const float h2 = (float)(dt / 2.), h1 = (float)dt, w6 = (float)(dt / 6.);
-    k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(b.yhi, L.P, 4), b, xa, pc, sc, h2, w6);
+#define EWPT_WALK nbx, nby, ycb
+    k_stage_fp32<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(b.yhi, L.P, 4), b, xa, pc, sc, h2, w6, EWPT_WALK);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, xb, pc, sc, h2, w6);
+    k_stage_fp32<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, xb, pc, sc, h2, w6, EWPT_WALK);
     launch_ghost_fill(g, L, xb, st, false);
-    k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xb, L.P, 4), b, xa, pc, sc, h1, w6);
+    k_stage_fp32<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xb, L.P, 4), b, xa, pc, sc, h1, w6, EWPT_WALK);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, nullptr, pc, sc, 0.f, w6);
+    k_stage_fp32<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack(xa, L.P, 4), b, nullptr, pc, sc, 0.f, w6, EWPT_WALK);
     launch_ghost_fill(g, L, b.yhi, st, false);
+#undef EWPT_WALK
 }
 
 template <bool BETA>

@@ -10,6 +10,8 @@
 // the ghosted layout (ewpt_internal.cuh), so neighbours past a face are read
 // from the ghost cells along y and z (refreshed by k_ghost_fill after each
 // stage) and wrapped in the offsets along x.  Needs nx even.
+#include <algorithm>
+
 #include "accessors.cuh"
 
 namespace {
@@ -61,11 +63,13 @@ struct PairSink {
 
 template <int STAGE, bool BETA, int REG>
 __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kMinBlocks)
-    k_stage_fp32x2(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X, PairBufs b, float* __restrict__ xn,
-                   PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6) {
-    const int ip = blockIdx.x * blockDim.x + threadIdx.x;  // pair index along x
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+    k_stage_fp32x2(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X,
+                   PairBufs b, float* __restrict__ xn, PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6, int nbx,
+                   int nby, int ycb) {
+    int bx, by, k;
+    chunk_walk(blockIdx.x, nbx, nby, g.nz, ycb, bx, by, k);
+    const int ip = bx * blockDim.x + threadIdx.x;  // pair index along x
+    const int j = by * blockDim.y + threadIdx.y;
     const int i0 = 2 * ip;
     if (i0 >= g.nx || j >= g.ny) return;
     PairAcc<SrcPtr36<float>> A{{X}};
@@ -85,16 +89,20 @@ template <bool BETA, int REG>
 void step_pair(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, float* xa, float* xb,
                const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
     const int npx = g.nx / 2;
-    const dim3 gr((npx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz), bl(t.bx, t.by);
+    const int nbx = (npx + t.bx - 1) / t.bx, nby = (g.ny + t.by - 1) / t.by;
+    const int ycb = std::max(1, kChunkRows / t.by);
+    const dim3 gr(nbx * nby * g.nz), bl(t.bx, t.by);
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
-    k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6);
+#define EWPT_PAIR_ARGS nbx, nby, ycb
+    k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6);
+    k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xb, st, false);
-    k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6);
+    k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6);
+    k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, b.yhi, st, false);
+#undef EWPT_PAIR_ARGS
 }
 
 template <bool BETA>

@@ -219,13 +219,16 @@ struct Ring {
     uint32_t tpar;           // parity offset of the current tile's boxes
     mutable int ok;          // no wait has run out
 
-    __device__ __forceinline__ static void origin(int t, int ntx_, int nty_, int& x, int& y, int& z) {
-        x = (t % ntx_) * BX;
-        y = ((t / ntx_) % nty_) * C::BY;
-        z = (t / (ntx_ * nty_)) * C::BZ;
+    // tile t of the chunked walk (chunk_walk, y chunks of kChunkRows rows)
+    __device__ __forceinline__ void origin(int t, int& x, int& y, int& z) const {
+        int tx, ty, tz;
+        chunk_walk(t, ntx, nty, ntiles / (ntx * nty), kChunkRows / C::BY, tx, ty, tz);
+        x = tx * BX;
+        y = ty * C::BY;
+        z = tz * C::BZ;
     }
     __device__ __forceinline__ void set_tile(int t, int iter) {
-        origin(t, ntx, nty, x0, y0, z0);
+        origin(t, x0, y0, z0);
         tpar = (uint32_t)(iter * (S::NLOAD / NS)) & 1u;
     }
 
@@ -278,7 +281,7 @@ struct Ring {
         int gq = 0;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
             int ox, oy, oz;
-            origin(t, ntx, nty, ox, oy, oz);
+            origin(t, ox, oy, oz);
             for (int j = 0; j < S::NLOAD; ++j, ++gq) {
                 if (gq >= NS && !mbar_wait(empty(j % NS), ((gq / NS) + 1) & 1)) {
                     ok = 0;

@@ -20,7 +20,7 @@ CANDIDATES = [(32, 4, 0, 0), (64, 2, 0, 0), (32, 2, 0, 0), (16, 8, 0, 0), (128, 
               (32, 4, 1, 0), (64, 2, 1, 0), (32, 2, 1, 0), (16, 8, 1, 0),
               (32, 4, 2, 0), (64, 2, 2, 0), (32, 2, 2, 0), (16, 8, 2, 0)]
 # FP32 form only: two sites per thread (needs even nx)
-PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (32, 1, 0, 1),
+PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (32, 1, 0, 1), (64, 1, 0, 1),
                    (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1)]
 # FP32 form only: TMA-staged tiles of 32 x by x bz sites, (bx, by, bz, 2)
 TMA_CANDIDATES = [(32, 4, 4, 2), (32, 2, 4, 2)]

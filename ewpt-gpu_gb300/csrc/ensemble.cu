@@ -159,7 +159,7 @@ struct ewpt_ens {
     EnsBufs b{};
     int64_t total = 0;  // sum of 36*S_m
     int64_t ntiles = 0;
-    int bx = 32, by = 4, pair = 0;
+    int bx = 8, by = 8, pair = 0;  // 8x8 pair-threads: the fastest shape for mixed 48-160 members
     bool beta = false;
     int grid = 0;
     cudaGraph_t graph = nullptr;

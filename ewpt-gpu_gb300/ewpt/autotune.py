@@ -114,7 +114,10 @@ def tune(lat: Lattice, steps: int = 2) -> tuple:
     return tile
 
 
-ENSEMBLE_CANDIDATES = [(32, 4, 1), (32, 2, 1), (64, 2, 1), (32, 1, 1), (32, 4, 0), (64, 2, 0), (32, 2, 0)]
+# (bx, by, pair); narrow blocks (8 or 16 pair-threads = 16 or 32 sites in x)
+# waste fewer threads on members of 48 / 96 / 160 sites per row
+ENSEMBLE_CANDIDATES = [(8, 8, 1), (8, 16, 1), (16, 8, 1), (16, 4, 1), (8, 4, 1), (32, 4, 1), (32, 2, 1), (64, 2, 1),
+                       (32, 4, 0), (16, 8, 0), (32, 2, 0)]
 
 
 def best_ensemble_tiling(members, steps: int = 2, use_cache: bool = True) -> tuple:

@@ -204,7 +204,8 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* ens, int32_t m, int32_t nb, const doubl
 /* constant Jex and gamma of member m for the following steps */
 int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
 /* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent
- * sites per thread (every member needs an even nx; default when possible) */
+ * sites per thread (every member needs an even nx; default when possible).
+ * Default 8x8 threads. */
 int ewpt_ensemble_set_tiling(ewpt_ens* ens, int32_t bx, int32_t by, int32_t pair);
 /* nsteps RK4 steps of every member, asynchronous on the ensemble's stream */
 int ewpt_ensemble_step(ewpt_ens* ens, int32_t nsteps);

@@ -39,7 +39,7 @@ int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx) {
                          p->nx, p->ny, p->nz);
     if ((int64_t)p->nx * p->ny * p->nz > (int64_t)INT32_MAX)
         return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large: nx*ny*nz must be < 2^31");
-    if (p->precision != EWPT_FP64 && p->precision != EWPT_FP32)
+    if (p->precision != EWPT_FP64 && p->precision != EWPT_FP32 && p->precision != EWPT_DF64)
         return ewpt_fail(ctx, EWPT_ERR_ARG, "precision %d unknown", p->precision);
     if (p->precision == EWPT_FP32 &&
         ghost_layout(Grid{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz}).P + 64 > (int64_t)INT32_MAX)
@@ -105,7 +105,7 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         return rc;
     }
     const size_t n = (size_t)36 * c->g.S;
-    if (p->precision == EWPT_FP64) {
+    if (p->precision == EWPT_FP64 || p->precision == EWPT_DF64) {
         e = cudaMalloc(&c->y, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->yn, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->xa, n * 8);
@@ -176,9 +176,9 @@ int ewpt_destroy(ewpt_ctx* c) {
 
 // Device buffer holding the packed FP64 state (for FP32 contexts, a staging
 // buffer that split/join convert through).
-static int staging64(ewpt_ctx* c, double** out) {
-    if (c->p.precision == EWPT_FP64) {
-        *out = c->y;
+static int staging64(ewpt_ctx* c, double** out, bool in) {
+    if (c->p.precision == EWPT_FP64 || (in && c->p.precision == EWPT_DF64)) {
+        *out = c->y;  // DF64: converted in place after the upload
         return EWPT_OK;
     }
     int rc = ewpt_ensure_scratch64(c);
@@ -194,7 +194,7 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
     cudaSetDevice(c->p.device);
     double* dst;
-    int rc = staging64(c, &dst);
+    int rc = staging64(c, &dst, true);
     if (rc) return rc;
     const size_t bytes = (size_t)c->g.S * 8;
     cudaError_t e = cudaSuccess;
@@ -202,6 +202,7 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
         e = cudaMemcpyAsync(dst + (size_t)a * c->g.S, arrays[a], bytes,
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st);
     if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, c->lay, dst, c->y32, c->st);
+    if (e == cudaSuccess && c->p.precision == EWPT_DF64) e = launch_to_dd(36 * c->g.S, c->y, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     return ewpt_cuda_check(c, e, "set_state");
 }
@@ -213,10 +214,11 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
     cudaSetDevice(c->p.device);
     double* src;
-    int rc = staging64(c, &src);
+    int rc = staging64(c, &src, false);
     if (rc) return rc;
     cudaError_t e = cudaSuccess;
     if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->lay, c->y32, src, c->st);
+    if (c->p.precision == EWPT_DF64) e = launch_from_dd(36 * c->g.S, c->y, src, c->st);
     const size_t bytes = (size_t)c->g.S * 8;
     for (int a = 0; a < 36 && e == cudaSuccess; ++a)
         e = cudaMemcpyAsync(arrays[a], src + (size_t)a * c->g.S, bytes,
@@ -264,6 +266,8 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         cudaError_t e;
         if (c->p.precision == EWPT_FP64)
             e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+        else if (c->p.precision == EWPT_DF64)
+            e = launch_step_dd(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
         else if (c->tile.pair == 2)
             e = launch_step_fp32_tma(c, J, G);
         else

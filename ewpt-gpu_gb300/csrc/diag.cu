@@ -317,9 +317,13 @@ int ewpt_state64(ewpt_ctx* c, const double** out) {
     }
     int rc = ewpt_ensure_scratch64(c);
     if (rc) return rc;
-    rc = ewpt_tma_check(c);
-    if (rc) return rc;
-    rc = ewpt_cuda_check(c, launch_fp32_join(c->g, c->lay, c->y32, c->scratch64, c->st), "join");
+    if (c->p.precision == EWPT_DF64) {
+        rc = ewpt_cuda_check(c, launch_from_dd(36 * c->g.S, c->y, c->scratch64, c->st), "join");
+    } else {
+        rc = ewpt_tma_check(c);
+        if (rc) return rc;
+        rc = ewpt_cuda_check(c, launch_fp32_join(c->g, c->lay, c->y32, c->scratch64, c->st), "join");
+    }
     if (rc) return rc;
     *out = c->scratch64;
     return EWPT_OK;

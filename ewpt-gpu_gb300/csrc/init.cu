@@ -132,12 +132,16 @@ extern "C" int ewpt_init_bubbles(ewpt_ctx* c, int32_t nb, const double* bubbles,
     cudaSetDevice(c->p.device);
     const double q0 = profile == EWPT_BUBBLE_REFERENCE ? c->p.mH : p0;
     std::string err;
-    rc = c->p.precision == EWPT_FP64
+    rc = c->p.precision != EWPT_FP32
              ? ewpt_launch_bubbles(c->g, c->p.dx, nb, bubbles, profile, q0, p1, c->p.vev, c->y, nullptr, nullptr,
                                    c->lay, c->st, &err)
              : ewpt_launch_bubbles(c->g, c->p.dx, nb, bubbles, profile, q0, p1, c->p.vev, nullptr, c->y32.hi,
                                    c->y32.lo, c->lay, c->st, &err);
     if (rc) return ewpt_fail(c, rc, "init_bubbles: %s", err.c_str());
+    if (c->p.precision == EWPT_DF64) {
+        rc = ewpt_cuda_check(c, launch_to_dd(36 * c->g.S, c->y, c->st), "init_bubbles");
+        if (rc) return rc;
+    }
     c->it = 0;
     return EWPT_OK;
 }

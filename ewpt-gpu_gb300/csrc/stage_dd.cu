@@ -1,0 +1,125 @@
+// stage_dd.cu -- DF64 form: the FP64 form's stage kernels (stage.cu) with
+// every stencil, flux and RK4 combination evaluated in double-float
+// arithmetic (dd.cuh) on the FP32 pipes.
+//
+// The state, the RK4 accumulator and the stage inputs keep the FP64 form's
+// buffers and scheme (y, yn, xa, xb, [36][S] of 8 bytes, the reference's
+// yn accumulation order, main_rk4.jl:6146-6437), each value stored as the
+// float pair (hi, lo).  State I/O converts from / to FP64 exactly
+// representable splits (hi = fl(v), lo = fl(v - hi)).
+#include "accessors.cuh"
+#include "dd.cuh"
+
+namespace {
+
+template <int REG>
+struct DdBudget;
+template <>
+struct DdBudget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
+template <>
+struct DdBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
+
+using DdAcc = SiteAcc<float2, dd, SrcPtr36<float2>>;
+
+template <int STAGE>
+struct DdSink {
+    const DdAcc& A;
+    const float2* __restrict__ y;
+    float2* yn;
+    float2* __restrict__ xn;
+    float2* acc_out;
+    int64_t S;
+    dd w, h;
+    __device__ __forceinline__ void operator()(int a, dd r) const {
+        const int64_t q = a * S + A.c;
+        if (STAGE == 1) {
+            const dd ya = A.v(a);  // X1 == y
+            yn[q] = (ya + w * r).f2();
+            xn[q] = (ya + h * r).f2();
+        } else if (STAGE < 4) {
+            // read then written by this thread only: read-only path is safe
+            yn[q] = (dd(__ldg(yn + q)) + w * r).f2();
+            xn[q] = (dd(__ldg(y + q)) + h * r).f2();
+        } else {
+            acc_out[q] = (dd(__ldg(yn + q)) + w * r).f2();
+        }
+    }
+};
+
+template <int STAGE, bool BETA, int REG>
+__global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBlocks)
+    k_stage_dd(Grid g, const __grid_constant__ Ptr36 X, const float2* __restrict__ y, float2* yn,
+               float2* __restrict__ xn, float2* acc_out, PhysCoef<dd> pc, StencilCoef<dd> sc, dd w, dd h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    DdAcc A{{X}};
+    A.place(i, j, k, g.nx, g.ny, g.nz);
+    A.s = sc;
+    DdSink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};
+    site_rates<dd, BETA>(A, pc, out);
+}
+
+__global__ void k_to_dd(int64_t n, double* __restrict__ v) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+        reinterpret_cast<float2*>(v)[q] = dd(v[q]).f2();
+}
+
+__global__ void k_from_dd(int64_t n, const double* __restrict__ src, double* __restrict__ dst) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2*>(src)[q];
+        dst[q] = (double)v.x + (double)v.y;
+    }
+}
+
+Ptr36 pack8(const void* base, int64_t S) {
+    Ptr36 P;
+    for (int a = 0; a < 36; ++a) P.p[a] = static_cast<const char*>(base) + (size_t)a * S * 8;
+    return P;
+}
+
+template <bool BETA, int REG>
+void step_dd(const Grid& g, const Tiling& t, float2* y, float2* yn, float2* xa, float2* xb, const PhysCoef<dd>& pc,
+             const StencilCoef<dd>& sc, double dt, cudaStream_t st) {
+    const dim3 gr((g.nx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz), bl(t.bx, t.by);
+    const dd w6(dt / 6.), w3(dt / 3.), h2(dt / 2.), h1(dt), z(0.0);
+    k_stage_dd<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(y, g.S), y, yn, xa, nullptr, pc, sc, w6, h2);
+    k_stage_dd<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xa, g.S), y, yn, xb, nullptr, pc, sc, w3, h2);
+    k_stage_dd<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xb, g.S), y, yn, xa, nullptr, pc, sc, w3, h1);
+    k_stage_dd<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xa, g.S), y, yn, nullptr, y, pc, sc, w6, z);
+}
+
+template <bool BETA>
+void step_dd_r(const Grid& g, const Tiling& t, float2* y, float2* yn, float2* xa, float2* xb, const PhysCoef<dd>& pc,
+               const StencilCoef<dd>& sc, double dt, cudaStream_t st) {
+    // the 128-register variant spills heavily in this form and runs as variant 0
+    if (t.reg == 2)
+        step_dd<BETA, 2>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+    else
+        step_dd<BETA, 0>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+}
+
+}  // namespace
+
+cudaError_t launch_step_dd(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
+                           const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+    const PhysCoef<dd> pc = make_phys<dd>(p, Jex, gam);
+    const StencilCoef<dd> sc = make_stencil<dd>(p.dx);
+    auto f2p = [](double* v) { return reinterpret_cast<float2*>(v); };
+    if (p.beta_w != 0.0 || p.beta_y != 0.0)
+        step_dd_r<true>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, st);
+    else
+        step_dd_r<false>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_dd(int64_t n, double* v, cudaStream_t st) {
+    k_to_dd<<<1216, 256, 0, st>>>(n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_dd(int64_t n, const double* src, double* dst, cudaStream_t st) {
+    k_from_dd<<<1216, 256, 0, st>>>(n, src, dst);
+    return cudaGetLastError();
+}

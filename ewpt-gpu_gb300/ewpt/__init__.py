@@ -6,10 +6,10 @@ parameters.jl, main_rk4.jl run()); the compute runs in libewpt.so through
 its C ABI (include/ewpt.h).
 """
 from . import _lib, ic
-from ._lib import FP32, FP64, EwptError, load
+from ._lib import DF64, FP32, FP64, EwptError, load
 from .ensemble import Ensemble
 from .lattice import DIAG_NAMES, Lattice, kc_bin_nums, rk4_rates_device
 from .params import Params, baseline_couplings
 
-__all__ = ["Ensemble", "Lattice", "Params", "baseline_couplings", "ic", "FP32", "FP64", "EwptError", "load",
+__all__ = ["Ensemble", "Lattice", "Params", "baseline_couplings", "ic", "FP32", "FP64", "DF64", "EwptError", "load",
            "DIAG_NAMES", "kc_bin_nums", "rk4_rates_device", "_lib"]

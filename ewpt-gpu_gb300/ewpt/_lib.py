@@ -18,7 +18,7 @@ NARR = 36
 NDIAG = 20
 
 OK, ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_STATE = range(8)
-FP64, FP32 = 0, 1
+FP64, FP32, DF64 = 0, 1, 2
 FIELD_B, FIELD_B2, FIELD_HIGGS = 0, 1, 2
 BUBBLE_REFERENCE, BUBBLE_TANH = 0, 1
 SPEC_LOG, SPEC_UNIQUE = 0, 1

@@ -47,7 +47,9 @@ enum ewpt_status {
 
 enum ewpt_precision {
     EWPT_FP64 = 0, /* stencils, fluxes, state and reductions in FP64 */
-    EWPT_FP32 = 1  /* FP32 stencils and fluxes; compensated FP32 hi/lo RK4 state; FP64 reductions */
+    EWPT_FP32 = 1, /* FP32 stencils and fluxes; compensated FP32 hi/lo RK4 state; FP64 reductions */
+    EWPT_DF64 = 2  /* the FP64 form evaluated in double-float (float hi + lo) arithmetic on the
+                      FP32 pipes: ~2^-47 per operation, FP64 reductions */
 };
 
 /* Parameter set.  Mirrors gpu-kernels-rk4/parameters.jl:1-98 (couplings,

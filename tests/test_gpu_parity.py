@@ -94,6 +94,41 @@ def test_fp64_100_steps_vs_oracle(shape, beta):
     assert rel_err(y, yo) < 1e-11
 
 
+@pytest.mark.parametrize("shape,beta", [((20, 24, 16), True), ((32, 32, 32), False)])
+def test_df64_100_steps_vs_oracle(shape, beta):
+    """The DF64 form (FP64 scheme in double-float arithmetic on the FP32
+    pipes) meets the FP64 parity bar: 1e-11 relative per field after 100
+    steps, with beta terms, J_ext and damping."""
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, precision=ewpt.DF64,
+                                beta_w=0.3 if beta else 0.0, beta_y=0.2 if beta else 0.0)
+    y0 = perturbed_bubbles(shape, p.dx, 4, seed=11)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        lat.step(100, Jex=0.02, gamma=0.01)
+        y = lat.get_state()
+        d = lat.diagnostics()
+    yo = orc.rk4_step(oparams(p), y0, p.dt, 0.02, 0.01, nsteps=100)
+    assert np.isfinite(y).all()
+    assert rel_err(y, yo) < 1e-11
+    do = orc.diagnostics(oparams(p), yo)
+    np.testing.assert_allclose(d[:14], do[:14], rtol=1e-9, atol=1e-12)
+
+
+def test_df64_state_roundtrip_and_golden_step(golden_dir):
+    """set_state / get_state of a DF64 context is exact to the double-float
+    split (2^-48), and one DF64 step matches the golden FP64 step to 1e-12."""
+    g = golden(golden_dir, "a")
+    p = params_from_golden(g)
+    p.precision = ewpt.DF64
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(g["y0"])
+        back = lat.get_state()
+        assert rel_err(back, g["y0"]) < 1e-14
+        lat.step(1, Jex=float(g["Jex"]), gamma=float(g["gam"]))
+        y1 = lat.get_state()
+    assert rel_err(y1, g["y1"]) < 1e-12
+
+
 def test_step_schedule_jext_damp():
     """ewpt_step applies J_ext/damp per iteration (main_rk4.jl:5154-5172)."""
     shape = (16, 16, 16)

@@ -25,6 +25,17 @@ import numpy as np
 
 from .params import Params
 
+try:  # multithreaded FFTs when scipy is present (same pocketfft algorithm)
+    import scipy.fft as _sfft
+
+    def _fftn(a):
+        return _sfft.fftn(a, workers=-1)
+
+    def _ifftn(a):
+        return _sfft.ifftn(a, workers=-1)
+except ImportError:  # pragma: no cover
+    _fftn, _ifftn = np.fft.fftn, np.fft.ifftn
+
 
 def _grid(shape, dx):
     nx, ny, nz = shape
@@ -150,19 +161,19 @@ def _real_field(rng, amp, shape):
     """real(bfft(amp * (r + i r')))/1 with r, r' ~ N(0, sqrt 2) per mode, the
     construction of main_rk4.jl:5352-5600 (unnormalised backward FFT)."""
     z = amp * (rng.normal(0.0, math.sqrt(2.0), amp.shape) + 1j * rng.normal(0.0, math.sqrt(2.0), amp.shape))
-    return np.real(np.fft.ifftn(z) * z.size)
+    return np.real(_ifftn(z) * z.size)
 
 
 def _grad(f, sym):
-    F = np.fft.fftn(f)
-    return [np.real(np.fft.ifftn(1j * s * F)) for s in sym]
+    F = _fftn(f)
+    return [np.real(_ifftn(1j * s * F)) for s in sym]
 
 
 def _div(fx, fy, fz, sym):
     out = 0
     for f, s in zip((fx, fy, fz), sym):
-        out = out + np.fft.fftn(f) * (1j * s)
-    return np.real(np.fft.ifftn(out))
+        out = out + _fftn(f) * (1j * s)
+    return np.real(_ifftn(out))
 
 
 def thermal(shape, dx, T=1.5, lam=0.129, gw=0.65, gy=0.35, vev=1.0, seed=0, mH=None, mW=None,
@@ -226,7 +237,7 @@ def thermal(shape, dx, T=1.5, lam=0.129, gw=0.65, gy=0.35, vev=1.0, seed=0, mH=N
         comps = []
         for i in range(3):
             z = amp * (e1[i] * xs[0] + e2[i] * xs[1])
-            comps.append(np.real(np.fft.ifftn(z) * z.size))
+            comps.append(np.real(_ifftn(z) * z.size))
         return comps
 
     S = nx * ny * nz
@@ -309,34 +320,70 @@ def _null_patterns(shape):
     return pats
 
 
+def _class_sums(f, shape):
+    """Sums of f over the 8 parity classes (k % 2, j % 2, i % 2) of the sites."""
+    nx, ny, nz = shape
+    a = f.reshape(nz, ny, nx)
+    return np.array([[[a[pz::2, py::2, px::2].sum() for px in (0, 1)] for py in (0, 1)] for pz in (0, 1)])
+
+
+def _null_vectors(shape):
+    """The e in {0,1}^3 (e_i = 1 only on even axes) of the staggered null
+    patterns (-1)^(e.x), in the order of _null_patterns."""
+    nx, ny, nz = shape
+    return [(ez, ey, ex) for ez in ((0, 1) if nz % 2 == 0 else (0,)) for ey in ((0, 1) if ny % 2 == 0 else (0,))
+            for ex in ((0, 1) if nx % 2 == 0 else (0,))]
+
+
+def _moment(s, e):
+    """sum_x (-1)^(e.x) f(x) from the parity-class sums s of f."""
+    return sum((-1.0) ** (e[0] * pz + e[1] * py + e[2] * px) * s[pz, py, px]
+               for pz in (0, 1) for py in (0, 1) for px in (0, 1))
+
+
 def neutralize_charges(y, gw, gy, shape):
     """Shift the Higgs momenta along the four charge generators so that the
     charges have no component in the null modes of the central-difference
     divergence (the zero mode and the Nyquist corners, where d_i E_i is 0
-    whatever E is): Gauss's law can only hold for such a charge density."""
+    whatever E is): Gauss's law can only hold for such a charge density.
+
+    Unknowns alpha[b, e]: pi += sum_b (sum_e alpha[b,e] (-1)^(e.x)) M_b^T phi.
+    Since (-1)^(e.x) (-1)^(e'.x) = (-1)^((e^e').x), every coefficient of the
+    linear system is a parity-class moment of one site field, so the system
+    costs 16 + 4 passes over the lattice."""
+    nx, ny, nz = shape
     rho, rhoY = gauss_charges(y, gw, gy)
     dens = list(rho) + [rhoY]
     coup = [gw, gw, gw, gy]
-    pats = _null_patterns(shape)
+    es = _null_vectors(shape)
+    ne = len(es)
     phi = y[0:4]
     Ms = [_charge_matrix(a) for a in range(4)]
     MT_phi = [M.T @ phi for M in Ms]
-    # unknowns alpha[b, P]: pi += alpha[b,P] * P(x) * M_b^T phi
-    n = 4 * len(pats)
+    n = 4 * ne
     A = np.zeros((n, n))
     Q = np.zeros(n)
     for a in range(4):
-        for pi_, P in enumerate(pats):
-            r = a * len(pats) + pi_
-            Q[r] = np.sum(P * dens[a])
-            for b in range(4):
-                g = coup[a] * np.sum(phi * (Ms[a] @ MT_phi[b]), axis=0)  # per-site phi^T M_a M_b^T phi
-                for pj, P2 in enumerate(pats):
-                    A[r, b * len(pats) + pj] = np.sum(P * P2 * g)
+        sq = _class_sums(dens[a], shape)
+        for pi_, e in enumerate(es):
+            Q[a * ne + pi_] = _moment(sq, e)
+        for b in range(4):
+            g = coup[a] * np.sum(phi * (Ms[a] @ MT_phi[b]), axis=0)  # per-site phi^T M_a M_b^T phi
+            sg = _class_sums(g, shape)
+            for pi_, e in enumerate(es):
+                for pj, e2 in enumerate(es):
+                    A[a * ne + pi_, b * ne + pj] = _moment(sg, tuple(u ^ v for u, v in zip(e, e2)))
     alpha = np.linalg.lstsq(A, -Q, rcond=None)[0]
+    # coefficient field of generator b: constant on each parity class
+    cls = ((np.arange(nz) % 2)[:, None, None] * 4 + (np.arange(ny) % 2)[None, :, None] * 2 +
+           (np.arange(nx) % 2)[None, None, :]).ravel()
     for b in range(4):
-        for pj, P2 in enumerate(pats):
-            y[20:24] += alpha[b * len(pats) + pj] * P2 * MT_phi[b]
+        table = np.zeros(8)
+        for c in range(8):
+            pz, py, px = c >> 2, (c >> 1) & 1, c & 1
+            table[c] = sum(alpha[b * ne + pj] * (-1.0) ** (e[0] * pz + e[1] * py + e[2] * px)
+                           for pj, e in enumerate(es))
+        y[20:24] += table[cls] * MT_phi[b]
     return y
 
 
@@ -357,9 +404,9 @@ def gauss_project(y, shape, dx, gw, gy, iters=12, sym=None):
         groups = [(24 + 3 * a, rho[a]) for a in range(3)] + [(33, rhoY)]
         for base, r in groups:
             Ex, Ey, Ez = (y[base + i].reshape(nz, ny, nx) for i in range(3))
-            F = [np.fft.fftn(Ex), np.fft.fftn(Ey), np.fft.fftn(Ez)]
-            res = 1j * (sym[0] * F[0] + sym[1] * F[1] + sym[2] * F[2]) - np.fft.fftn(r.reshape(nz, ny, nx))
+            F = [_fftn(Ex), _fftn(Ey), _fftn(Ez)]
+            res = 1j * (sym[0] * F[0] + sym[1] * F[1] + sym[2] * F[2]) - _fftn(r.reshape(nz, ny, nx))
             chi = np.where(ok, res / np.where(ok, -s2, 1.0), 0.0)
             for i in range(3):
-                y[base + i] = np.real(np.fft.ifftn(F[i] - 1j * sym[i] * chi)).ravel()
+                y[base + i] = np.real(_ifftn(F[i] - 1j * sym[i] * chi)).ravel()
     return y

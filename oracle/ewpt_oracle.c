@@ -40,28 +40,78 @@
 
 #define NARR 36
 
+/* order: finite-difference order of every stencil (0 or 6: the driver's
+ * `differentiations`, diff_scheme.jl:157-311; 2, 8, 10, 12: the modules
+ * differentiations_{2nd,8th,10th,12th}_order, diff_scheme.jl:370-1438);
+ * -2: the 2nd-order module exactly as written, whose branches miss the
+ * planes i = 2 and i = N-1 (1-based), where it returns the caller's
+ * placeholder 0 (every call site passes 0.). */
 typedef struct or_params {
-    int32_t nx, ny, nz, pad_;
+    int32_t nx, ny, nz, order;
     double dx, gw, gy, gp2, lambda, vev, beta_w, beta_y, theta_w;
 } or_params;
 
 /* ---------------------------------------------------------------- stencils */
-/* diff_scheme.jl:157-233.  The seven branches there are a periodic wrap of
- * the 7-point stencil; the formula is identical in every branch. */
-typedef struct { int64_t p1, p2, p3, m1, m2, m3; } nbr_t;
+/* diff_scheme.jl:157-233 (and 376-1403 for the other orders).  The
+ * branches of each function there are a periodic wrap of one stencil; the
+ * formula is identical in every branch, so the neighbours below are wrapped
+ * indices and each formula keeps the written evaluation order. */
+typedef struct {
+    int64_t p[6], m[6]; /* +1..+6, -1..-6 */
+    int gap;            /* order -2 at 1-based index 2 or N-1: the reference returns 0 */
+} nbr_t;
+
+static int g_order = 6; /* the stencil order in force (or_params.order, 0 -> 6) */
 
 static inline int wrap(int i, int n) { i %= n; return i < 0 ? i + n : i; }
 
+static void use_order(const or_params* p) { g_order = p->order ? p->order : 6; }
+
+#define P_(d) A[s->p[(d) - 1]]
+#define M_(d) A[s->m[(d) - 1]]
 static inline double d1(const double* A, int64_t c, const nbr_t* s, double dx) {
     (void)c;
-    return (A[s->p3] - 9. * A[s->p2] + 45. * A[s->p1] -
-            45. * A[s->m1] + 9. * A[s->m2] - A[s->m3]) / (60 * dx);
+    switch (g_order) {
+        case 2:
+        case -2: /* diff_scheme.jl:1372-1381 */
+            if (s->gap) return 0.;
+            return (-M_(1) + P_(1)) / (2.0 * dx);
+        case 8: /* diff_scheme.jl:376-415 */
+            return (3 * M_(4) - 32 * M_(3) + 168 * M_(2) - 672 * M_(1) + 672 * P_(1) - 168 * P_(2) + 32 * P_(3) -
+                    3 * P_(4)) / (840 * dx);
+        case 10: /* diff_scheme.jl:633-680 */
+            return (-2 * M_(5) + 25 * M_(4) - 150 * M_(3) + 600 * M_(2) - 2100 * M_(1) + 2100 * P_(1) - 600 * P_(2) +
+                    150 * P_(3) - 25 * P_(4) + 2 * P_(5)) / (2520 * dx);
+        case 12: /* diff_scheme.jl:939-1007 */
+            return (5 * M_(6) - 72 * M_(5) + 495 * M_(4) - 2200 * M_(3) + 7425 * M_(2) - 23760 * M_(1) +
+                    23760 * P_(1) - 7425 * P_(2) + 2200 * P_(3) - 495 * P_(4) + 72 * P_(5) - 5 * P_(6)) / (27720 * dx);
+        default: /* diff_scheme.jl:157-181 */
+            return (P_(3) - 9. * P_(2) + 45. * P_(1) - 45. * M_(1) + 9. * M_(2) - M_(3)) / (60 * dx);
+    }
 }
-/* diff_scheme.jl:235-311 */
 static inline double d2(const double* A, int64_t c, const nbr_t* s, double dx) {
-    return (A[s->p3] / 90. - 3. * A[s->p2] / 20. + 3. * A[s->p1] / 2. -
-            49. * A[c] / 18. + 3. * A[s->m1] / 2. - 3. * A[s->m2] / 20. + A[s->m3] / 90.) / (dx * dx);
+    switch (g_order) {
+        case 2:
+        case -2: /* diff_scheme.jl:1405-1414 */
+            if (s->gap) return 0.;
+            return (M_(1) - 2.0 * A[c] + P_(1)) / (dx * dx);
+        case 8: /* diff_scheme.jl:499-538 */
+            return (-9 * M_(4) + 128 * M_(3) - 1008 * M_(2) + 8064 * M_(1) - 14350 * A[c] + 8064 * P_(1) -
+                    1008 * P_(2) + 128 * P_(3) - 9 * P_(4)) / (5040 * dx * dx);
+        case 10: /* diff_scheme.jl:780-827 */
+            return (8 * M_(5) - 125 * M_(4) + 1000 * M_(3) - 6000 * M_(2) + 42000 * M_(1) - 73766 * A[c] +
+                    42000 * P_(1) - 6000 * P_(2) + 1000 * P_(3) - 125 * P_(4) + 8 * P_(5)) / (25200 * dx * dx);
+        case 12: /* diff_scheme.jl:1149-1217 */
+            return (-50 * M_(6) + 864 * M_(5) - 7425 * M_(4) + 44000 * M_(3) - 222750 * M_(2) + 1425600 * M_(1) -
+                    2480478 * A[c] + 1425600 * P_(1) - 222750 * P_(2) + 44000 * P_(3) - 7425 * P_(4) +
+                    864 * P_(5) - 50 * P_(6)) / (831600 * dx * dx);
+        default: /* diff_scheme.jl:235-259 */
+            return (P_(3) / 90. - 3. * P_(2) / 20. + 3. * P_(1) / 2. - 49. * A[c] / 18. + 3. * M_(1) / 2. -
+                    3. * M_(2) / 20. + M_(3) / 90.) / (dx * dx);
+    }
 }
+#undef P_
+#undef M_
 
 typedef struct {
     int64_t c;
@@ -69,19 +119,24 @@ typedef struct {
 } site_t;
 
 static inline void make_site(const or_params* p, int i, int j, int k, site_t* s) {
-    const int64_t nx = p->nx, ny = p->ny, nz = p->nz;
-    const int64_t sy = nx, sz = nx * ny;
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
     const int64_t base_yz = (int64_t)j * sy + (int64_t)k * sz;
     const int64_t base_xz = (int64_t)i + (int64_t)k * sz;
     const int64_t base_xy = (int64_t)i + (int64_t)j * sy;
     s->c = i + base_yz;
-    s->x.p1 = wrap(i + 1, nx) + base_yz; s->x.p2 = wrap(i + 2, nx) + base_yz; s->x.p3 = wrap(i + 3, nx) + base_yz;
-    s->x.m1 = wrap(i - 1, nx) + base_yz; s->x.m2 = wrap(i - 2, nx) + base_yz; s->x.m3 = wrap(i - 3, nx) + base_yz;
-    s->y.p1 = wrap(j + 1, ny) * sy + base_xz; s->y.p2 = wrap(j + 2, ny) * sy + base_xz; s->y.p3 = wrap(j + 3, ny) * sy + base_xz;
-    s->y.m1 = wrap(j - 1, ny) * sy + base_xz; s->y.m2 = wrap(j - 2, ny) * sy + base_xz; s->y.m3 = wrap(j - 3, ny) * sy + base_xz;
-    s->z.p1 = wrap(k + 1, nz) * sz + base_xy; s->z.p2 = wrap(k + 2, nz) * sz + base_xy; s->z.p3 = wrap(k + 3, nz) * sz + base_xy;
-    s->z.m1 = wrap(k - 1, nz) * sz + base_xy; s->z.m2 = wrap(k - 2, nz) * sz + base_xy; s->z.m3 = wrap(k - 3, nz) * sz + base_xy;
-    (void)nz;
+    for (int d = 1; d <= 6; ++d) {
+        s->x.p[d - 1] = wrap(i + d, nx) + base_yz;
+        s->x.m[d - 1] = wrap(i - d, nx) + base_yz;
+        s->y.p[d - 1] = wrap(j + d, ny) * sy + base_xz;
+        s->y.m[d - 1] = wrap(j - d, ny) * sy + base_xz;
+        s->z.p[d - 1] = wrap(k + d, nz) * sz + base_xy;
+        s->z.m[d - 1] = wrap(k - d, nz) * sz + base_xy;
+    }
+    const int g2 = g_order == -2;
+    s->x.gap = g2 && (i == 1 || i == nx - 2);
+    s->y.gap = g2 && (j == 1 || j == ny - 2);
+    s->z.gap = g2 && (k == 1 || k == nz - 2);
 }
 
 #define DX(A) d1((A), s.c, &s.x, dx)
@@ -465,6 +520,7 @@ static void splitw(const or_params* p, double* base, double** v) {
 /* Rates of the 36 arrays: one application of rk4_step!.  y and r are
  * contiguous [36][S] buffers and must not alias. */
 int or_rates(const or_params* p, const double* y, double* r, double Jex, double gam) {
+    use_order(p);
     if (!p || !y || !r || p->nx < 7 || p->ny < 7 || p->nz < 7) return 1;
     const double* yv[NARR];
     double* rv[NARR];
@@ -492,6 +548,7 @@ double or_damp(int64_t it, double dt, double mH, double t_sat, int thermal, doub
  * X = k*(dt/6) + X_n; stage arguments X + k*(dt/2), X + k*(dt/2), X + k*dt.
  * work must hold 3*36*S doubles. */
 int or_rk4_step(const or_params* p, double* y, double* work, double dt, double Jex, double gam) {
+    use_order(p);
     if (!p || !y || !work) return 1;
     const int64_t n = NARR * nsites(p);
     double* kk = work;
@@ -642,6 +699,7 @@ int or_ndensities(void) { return NDEN; }
 
 /* Per-site density fields, [NDEN][S]. */
 int or_densities(const or_params* p, const double* y, double* out) {
+    use_order(p);
     if (!p || !y || !out || p->nx < 7 || p->ny < 7 || p->nz < 7) return 1;
     const double* yv[NARR];
     split(p, y, yv);
@@ -666,6 +724,7 @@ int or_densities(const or_params* p, const double* y, double* out) {
 int or_ndiag(void) { return NDIAG; }
 
 int or_diagnostics(const or_params* p, const double* y, double* out) {
+    use_order(p);
     const int64_t S = nsites(p);
     double* den = (double*)malloc(sizeof(double) * NDEN * S);
     if (!den) return 2;

@@ -33,7 +33,7 @@ DENSITY_NAMES = ["PE", "KE", "GE", "EEW", "MEW", "EEY", "MEY", "Bx", "By", "Bz",
 
 
 class OrParams(C.Structure):
-    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("pad_", C.c_int32),
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("order", C.c_int32),
                 ("dx", C.c_double), ("gw", C.c_double), ("gy", C.c_double), ("gp2", C.c_double),
                 ("lam", C.c_double), ("vev", C.c_double), ("beta_w", C.c_double),
                 ("beta_y", C.c_double), ("theta_w", C.c_double)]
@@ -80,9 +80,11 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def params(shape, dx, gw, gy, gp2, lam, vev, beta_w=0.0, beta_y=0.0, theta_w=0.0) -> OrParams:
+def params(shape, dx, gw, gy, gp2, lam, vev, beta_w=0.0, beta_y=0.0, theta_w=0.0, order=6) -> OrParams:
+    """order: stencil order 2, 6, 8, 10 or 12; -2 = the reference's 2nd-order
+    module as written (derivatives 0 on the planes i = 2 and N-1, 1-based)."""
     nx, ny, nz = shape
-    return OrParams(nx, ny, nz, 0, dx, gw, gy, gp2, lam, vev, beta_w, beta_y, theta_w)
+    return OrParams(nx, ny, nz, int(order), dx, gw, gy, gp2, lam, vev, beta_w, beta_y, theta_w)
 
 
 def rates(p: OrParams, y: np.ndarray, Jex: float = 0.0, gamma: float = 0.0) -> np.ndarray:

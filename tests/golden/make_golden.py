@@ -11,6 +11,7 @@ precision on seeded inputs:
 
   rk4_step!                      gpu-kernels-rk4/main_rk4.jl:52-661
   dfdx..d2fdz2 (6th order)       gpu-kernels-rk4/diff_scheme.jl:157-311
+  the 2nd/8th/10th/12th-order modules   gpu-kernels-rk4/diff_scheme.jl:370-1438
   D_2phi_a..D_4phi_a             gpu-kernels-rk4/cov_derivs_temporal.jl:23-130
   W_a_xy.., Y_2_y..              gpu-kernels-rk4/field_strengths.jl:34-311
   compute_PE!..compute_Az!       gpu-kernels-rk4/main_rk4.jl:1334-4250
@@ -190,6 +191,56 @@ def spectrum_case(ns, seed=7):
     print("spectrum bins", nb)
 
 
+# modules differentiations_{8th,10th,12th,2nd}_order of diff_scheme.jl
+ORDER_MODULES = {8: (370, 626), 10: (627, 932), 12: (933, 1365), 2: (1366, 1438)}
+
+
+def orders_case(ref, ns):
+    """rk4_step! rates with each alternative stencil module swapped in (the
+    driver selects one by `using`, main_rk4.jl:33-35), on a 14^3 lattice so
+    that the 12th-order branches (diff_scheme.jl:939-1403) stay distinct;
+    plus the snapshot densities with the 8th-order module."""
+    base = os.path.join(ref, "gpu-kernels-rk4")
+    shape = (14, 14, 14)
+    rng = np.random.default_rng(4321)
+    y0 = random_state(rng, shape)
+    tw = math.asin(math.sqrt(0.22))
+    params = dict(gw=0.65, gy=0.35, gp2=0.99, vev=1.0, dx=0.3, beta_w=0.3, beta_y=0.2, theta_w=tw)
+    params["lambda"] = 0.129
+    sc = dict(gw=params["gw"], gy=params["gy"], gp2=params["gp2"], beta_W=params["beta_w"],
+              beta_Y=params["beta_y"], vev=params["vev"], lambda_=params["lambda"], dx=params["dx"],
+              theta_w=params["theta_w"])
+    out = dict(shape=np.array(shape), y0=y0, Jex=0.07, gam=0.05, **{f"p_{k}": v for k, v in params.items()})
+    diff_src = os.path.join(base, "diff_scheme.jl")
+    # diff_scheme.jl:879: the 10th-order d2fdz2 tests `i` instead of `k` in its
+    # interior branch, so on the z-boundary planes it indexes outside the
+    # array; the fixture uses the intended condition (one token changed).
+    with open(diff_src, encoding="utf-8") as f:
+        text = f.read().split("\n")
+    bad = "    if (i>5 && i<(size(A,3)-4))"
+    assert text[878] == bad, text[878]
+    text[878] = "    if (k>5 && k<(size(A,3)-4))"
+    fixed = os.path.join(HERE, "_diff_scheme_fixed.jl")
+    with open(fixed, "w", encoding="utf-8") as f:
+        f.write("\n".join(text))
+    for order, lines in ORDER_MODULES.items():
+        nso = dict(ns)
+        js.load_functions(fixed, ["dfdx", "dfdy", "dfdz", "d2fdx2", "d2fdy2", "d2fdz2"], nso, lines)
+        # the kernels resolve the stencils through the namespace they were loaded into
+        js.load_functions(os.path.join(base, "main_rk4.jl"), ["rk4_step!"] + DENSITY_KERNELS, nso)
+        js.load_functions(os.path.join(base, "cov_derivs_temporal.jl"),
+                          [f"D_{i}ϕ_{a}" for i in (2, 3, 4) for a in (1, 2, 3, 4)], nso)
+        js.load_functions(os.path.join(base, "field_strengths.jl"),
+                          [f"W_{a}_{p}" for a in (1, 2, 3) for p in ("xy", "xz", "yz")]
+                          + ["Y_2_y", "Y_2_z", "Y_3_z"], nso)
+        out[f"rates_{order}"] = rates(nso, y0, shape, sc, 0.07, 0.05)
+        if order == 8:
+            out["dens_8"] = densities(nso, y0, shape, sc)
+        print("order", order, "rates", np.abs(out[f"rates_{order}"]).max(), flush=True)
+    os.remove(fixed)
+    np.savez_compressed(os.path.join(HERE, "ref_orders.npz"), **out)
+
+
 def bubble_case(ns):
     shape = (8, 8, 8)
     S = int(np.prod(shape))
@@ -232,6 +283,7 @@ def main():
     case(ns, "b", (7, 8, 9), pb, dt=0.05, Jex=0.0, gam=0.0, seed=99)
     spectrum_case(ns)
     bubble_case(ns)
+    orders_case(ref, ns)
 
 
 if __name__ == "__main__":

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "ewpt_ctx.cuh"
+#include "stencil_n.cuh"
 
 static thread_local std::string g_err = "";
 
@@ -41,6 +42,15 @@ int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx) {
         return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large: nx*ny*nz must be < 2^31");
     if (p->precision != EWPT_FP64 && p->precision != EWPT_FP32 && p->precision != EWPT_DF64)
         return ewpt_fail(ctx, EWPT_ERR_ARG, "precision %d unknown", p->precision);
+    {
+        const int ord = p->stencil_order ? p->stencil_order : 6;
+        const int R = stencil_radius(ord);
+        if (R == 0) return ewpt_fail(ctx, EWPT_ERR_ARG, "stencil order %d unknown (2, 6, 8, 10 or 12)", ord);
+        if (ord != 6 && p->precision != EWPT_FP64)
+            return ewpt_fail(ctx, EWPT_ERR_ARG, "stencil order %d needs the FP64 form", ord);
+        if (p->nx < 2 * R + 1 || p->ny < 2 * R + 1 || p->nz < 2 * R + 1)
+            return ewpt_fail(ctx, EWPT_ERR_ARG, "stencil order %d needs >= %d sites per axis", ord, 2 * R + 1);
+    }
     if (p->precision == EWPT_FP32 &&
         ghost_layout(Grid{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz}).P + 64 > (int64_t)INT32_MAX)
         return ewpt_fail(ctx, EWPT_ERR_ARG, "lattice too large for the FP32 form's padded arrays (< 2^31 cells)");
@@ -75,6 +85,7 @@ int ewpt_params_default(ewpt_params* p, int32_t n) {
     p->t_sat = 2.0;
     p->thermal_init = 0;
     p->device = 0;
+    p->stencil_order = 6;
     return EWPT_OK;
 }
 
@@ -92,6 +103,7 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         return ewpt_fail(nullptr, EWPT_ERR_ARG, "device %d out of range (%d devices)", p->device, ndev);
     ewpt_ctx* c = new ewpt_ctx();
     c->p = *p;
+    if (!c->p.stencil_order) c->p.stencil_order = 6;
     c->g.nx = p->nx;
     c->g.ny = p->ny;
     c->g.nz = p->nz;
@@ -138,6 +150,7 @@ int ewpt_create_view(const ewpt_params* p, ewpt_ctx** out) {
     if (rc) return rc;
     ewpt_ctx* c = new ewpt_ctx();
     c->p = *p;
+    if (!c->p.stencil_order) c->p.stencil_order = 6;
     c->p.precision = EWPT_FP64;
     c->g = Grid{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz};
     c->view = true;
@@ -264,7 +277,9 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         const double J = expl ? Jex : jext_of(c->p, it);
         const double G = expl ? gam : damp_of(c->p, it);
         cudaError_t e;
-        if (c->p.precision == EWPT_FP64)
+        if (c->p.precision == EWPT_FP64 && c->p.stencil_order != 6)
+            e = launch_step_fp64_order(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+        else if (c->p.precision == EWPT_FP64)
             e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
         else if (c->p.precision == EWPT_DF64)
             e = launch_step_dd(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
@@ -351,7 +366,10 @@ int ewpt_rk4_rates(const ewpt_params* p, const double* const in[EWPT_NARR], doub
     if (!std::isfinite(Jex) || !std::isfinite(gamma)) return ewpt_fail(nullptr, EWPT_ERR_ARG, "non-finite Jex/gamma");
     Grid g{p->nx, p->ny, p->nz, (int64_t)p->nx * p->ny * p->nz};
     cudaError_t e = cudaSetDevice(p->device);
-    if (e == cudaSuccess) e = launch_rates_fp64(g, I, O, *p, Jex, gamma, (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = (p->stencil_order && p->stencil_order != 6)
+                ? launch_rates_fp64_order(g, I, O, *p, Jex, gamma, (cudaStream_t)stream)
+                : launch_rates_fp64(g, I, O, *p, Jex, gamma, (cudaStream_t)stream);
     return ewpt_cuda_check(nullptr, e, "rk4_rates");
 }
 

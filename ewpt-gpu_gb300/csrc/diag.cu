@@ -10,6 +10,7 @@
 #include <cmath>
 
 #include "ewpt_ctx.cuh"
+#include "stencil_n.cuh"
 
 namespace {
 
@@ -18,21 +19,24 @@ constexpr int DX_ = 32, DY_ = 4, DT = DX_ * DY_;
 struct DiagCoef {
     double gw, gy, hgw, hgy, lambda, vev2, sw, cw, bcoef;  // bcoef = 4 sin(th)/(gw vev^2)
     double four_sw_gw;                                      // 4 sin(th)/gw (B_2)
-    StencilCoef<double> s;
+    double a[6];                                            // first-derivative weights / dx (radius R)
 };
 
-// Neighbour access on an FP64 [36][S] buffer.
+// Neighbour access on an FP64 [36][S] buffer, stencil radius R.
+template <int R>
 struct DAcc {
     const double* __restrict__ y;
     int64_t S;
     int c;
-    int ox[6], oy[6], oz[6];
-    StencilCoef<double> s;
-    __device__ __forceinline__ double ld(int a, int off) const { return __ldg(y + a * S + c + off); }
-    __device__ __forceinline__ double v(int a) const { return ld(a, 0); }
-    __device__ __forceinline__ double d1(int a, const int* o) const {
-        return s.a1 * (ld(a, o[0]) - ld(a, o[3])) + s.a2 * (ld(a, o[1]) - ld(a, o[4])) +
-               s.a3 * (ld(a, o[2]) - ld(a, o[5]));
+    int ox[2 * R], oy[2 * R], oz[2 * R];
+    double a[R];
+    __device__ __forceinline__ double ld(int q, int off) const { return __ldg(y + q * S + c + off); }
+    __device__ __forceinline__ double v(int q) const { return ld(q, 0); }
+    __device__ __forceinline__ double d1(int q, const int* o) const {
+        double r = a[0] * (ld(q, o[0]) - ld(q, o[R]));
+#pragma unroll
+        for (int d = 1; d < R; ++d) r = r + a[d] * (ld(q, o[d]) - ld(q, o[R + d]));
+        return r;
     }
     __device__ __forceinline__ double dx(int a) const { return d1(a, ox); }
     __device__ __forceinline__ double dy(int a) const { return d1(a, oy); }
@@ -47,7 +51,8 @@ struct SiteDiag {
     double gw1, gw2, gw3, gy_, cw1, cw2, cw3, cy;
 };
 
-__device__ __forceinline__ void site_diag(const DAcc& A, const DiagCoef& k, SiteDiag& o) {
+template <class DA>
+__device__ __forceinline__ void site_diag(const DA& A, const DiagCoef& k, SiteDiag& o) {
     const double p1 = A.v(0), p2 = A.v(1), p3 = A.v(2), p4 = A.v(3);
     const double W12 = A.v(4), W13 = A.v(5), W14 = A.v(6);
     const double W22 = A.v(7), W23 = A.v(8), W24 = A.v(9);
@@ -153,17 +158,20 @@ __device__ __forceinline__ void site_diag(const DAcc& A, const DiagCoef& k, Site
 enum { R_PE = 0, R_KE, R_GE, R_EEW, R_MEW, R_EEY, R_MEY, R_BX, R_BY, R_BZ, R_B2X, R_B2Y, R_B2Z,
        R_MOD, R_HEL, R_GW, R_GY, R_CW, R_CY, NSUM, R_MIN = NSUM, R_MAXGW, R_MAXGY, NRED };
 
-__device__ __forceinline__ void make_dacc(const Grid& g, const double* y, const StencilCoef<double>& s, int i,
-                                          int j, int k, DAcc& A) {
+template <int R>
+__device__ __forceinline__ void make_dacc(const Grid& g, const double* y, const DiagCoef& kc, int i, int j, int k,
+                                          DAcc<R>& A) {
     A.y = y;
     A.S = g.S;
     A.c = i + g.nx * (j + g.ny * k);
-    axis_offsets(i, g.nx, 1, A.ox);
-    axis_offsets(j, g.ny, g.nx, A.oy);
-    axis_offsets(k, g.nz, g.nx * g.ny, A.oz);
-    A.s = s;
+    axis_offsets_n<R>(i, g.nx, 1, A.ox);
+    axis_offsets_n<R>(j, g.ny, g.nx, A.oy);
+    axis_offsets_n<R>(k, g.nz, g.nx * g.ny, A.oz);
+#pragma unroll
+    for (int d = 0; d < R; ++d) A.a[d] = kc.a[d];
 }
 
+template <int R>
 __global__ void __launch_bounds__(DT) k_diag_partial(Grid g, const double* __restrict__ y, DiagCoef kc,
                                                      double* __restrict__ part) {
     double acc[NRED];
@@ -176,8 +184,8 @@ __global__ void __launch_bounds__(DT) k_diag_partial(Grid g, const double* __res
     const int j = blockIdx.y * DY_ + threadIdx.y;
     if (i < g.nx && j < g.ny) {
         for (int k = blockIdx.z; k < g.nz; k += gridDim.z) {
-            DAcc A;
-            make_dacc(g, y, kc.s, i, j, k, A);
+            DAcc<R> A;
+            make_dacc<R>(g, y, kc, i, j, k, A);
             SiteDiag o;
             site_diag(A, kc, o);
             acc[R_PE] += o.pe;
@@ -256,6 +264,7 @@ __global__ void k_diag_final(const double* __restrict__ part, int nb, double* __
 
 // Writes one real field per component for the spectra: which = 0 -> B
 // (compute_Bx/By/Bz!), 1 -> B_2 (compute_B_2_*!), 2 -> Higgs phi_1..4.
+template <int R>
 __global__ void __launch_bounds__(DT) k_fields(Grid g, const double* __restrict__ y, DiagCoef kc, int which,
                                                double* __restrict__ f) {
     const int i = blockIdx.x * DX_ + threadIdx.x;
@@ -268,8 +277,8 @@ __global__ void __launch_bounds__(DT) k_fields(Grid g, const double* __restrict_
             for (int a = 0; a < 4; ++a) f[a * g.S + c] = y[a * g.S + c];
             continue;
         }
-        DAcc A;
-        make_dacc(g, y, kc.s, i, j, k, A);
+        DAcc<R> A;
+        make_dacc<R>(g, y, kc, i, j, k, A);
         SiteDiag o;
         site_diag(A, kc, o);
         f[c] = which == 0 ? o.bx : o.b2x;
@@ -290,8 +299,33 @@ DiagCoef diag_coef(const ewpt_params& p) {
     k.cw = std::cos(p.theta_w);
     k.bcoef = 4. * k.sw / (p.gw * (p.vev * p.vev));
     k.four_sw_gw = 4. * k.sw / p.gw;
-    k.s = make_stencil<double>(p.dx);
+    const int R = stencil_radius(p.stencil_order);
+    for (int d = 0; d < 6; ++d) k.a[d] = 0.0;
+    switch (R) {
+        case 1: { const auto s = make_stencil_n<double, 1>(p.dx); for (int d = 0; d < 1; ++d) k.a[d] = s.a[d]; break; }
+        case 4: { const auto s = make_stencil_n<double, 4>(p.dx); for (int d = 0; d < 4; ++d) k.a[d] = s.a[d]; break; }
+        case 5: { const auto s = make_stencil_n<double, 5>(p.dx); for (int d = 0; d < 5; ++d) k.a[d] = s.a[d]; break; }
+        case 6: { const auto s = make_stencil_n<double, 6>(p.dx); for (int d = 0; d < 6; ++d) k.a[d] = s.a[d]; break; }
+        default: {  // the 6th-order coefficients of the stage kernels
+            const StencilCoef<double> s = make_stencil<double>(p.dx);
+            k.a[0] = s.a1;
+            k.a[1] = s.a2;
+            k.a[2] = s.a3;
+        }
+    }
     return k;
+}
+
+void launch_partial(int R, dim3 gr, const Grid& g, const double* y, const DiagCoef& kc, double* part,
+                    cudaStream_t st) {
+    const dim3 bl(DX_, DY_);
+    switch (R) {
+        case 1: k_diag_partial<1><<<gr, bl, 0, st>>>(g, y, kc, part); break;
+        case 4: k_diag_partial<4><<<gr, bl, 0, st>>>(g, y, kc, part); break;
+        case 5: k_diag_partial<5><<<gr, bl, 0, st>>>(g, y, kc, part); break;
+        case 6: k_diag_partial<6><<<gr, bl, 0, st>>>(g, y, kc, part); break;
+        default: k_diag_partial<3><<<gr, bl, 0, st>>>(g, y, kc, part);
+    }
 }
 
 dim3 diag_grid(const Grid& g) {
@@ -353,7 +387,7 @@ static void finish_row(const ewpt_params& p, int64_t S, const double* r, double*
 cudaError_t launch_diag(const Grid& g, const ewpt_params& p, const double* y, double* part, double* dres,
                         cudaStream_t st) {
     const dim3 gr = diag_grid(g);
-    k_diag_partial<<<gr, dim3(DX_, DY_), 0, st>>>(g, y, diag_coef(p), part);
+    launch_partial(stencil_radius(p.stencil_order), gr, g, y, diag_coef(p), part, st);
     k_diag_final<<<1, 256, 0, st>>>(part, gr.x * gr.y * gr.z, dres);
     return cudaGetLastError();
 }
@@ -380,7 +414,7 @@ cudaError_t launch_diag_bounded(const Grid& g, const ewpt_params& p, const doubl
     if (bz > (int64_t)gr.z) bz = gr.z;
     if (bz < 1) bz = 1;
     gr.z = (unsigned)bz;
-    k_diag_partial<<<gr, dim3(DX_, DY_), 0, st>>>(g, y, diag_coef(p), part);
+    launch_partial(stencil_radius(p.stencil_order), gr, g, y, diag_coef(p), part, st);
     k_diag_final<<<1, 256, 0, st>>>(part, gr.x * gr.y * gr.z, dres);
     return cudaGetLastError();
 }
@@ -389,7 +423,15 @@ void diag_finish_row(const ewpt_params& p, int64_t S, const double* r, double* o
 
 cudaError_t launch_fields(const Grid& g, const ewpt_params& p, const double* y, int which, double* f,
                           cudaStream_t st) {
-    k_fields<<<diag_grid(g), dim3(DX_, DY_), 0, st>>>(g, y, diag_coef(p), which, f);
+    const dim3 gr = diag_grid(g), bl(DX_, DY_);
+    const DiagCoef kc = diag_coef(p);
+    switch (stencil_radius(p.stencil_order)) {
+        case 1: k_fields<1><<<gr, bl, 0, st>>>(g, y, kc, which, f); break;
+        case 4: k_fields<4><<<gr, bl, 0, st>>>(g, y, kc, which, f); break;
+        case 5: k_fields<5><<<gr, bl, 0, st>>>(g, y, kc, which, f); break;
+        case 6: k_fields<6><<<gr, bl, 0, st>>>(g, y, kc, which, f); break;
+        default: k_fields<3><<<gr, bl, 0, st>>>(g, y, kc, which, f);
+    }
     return cudaGetLastError();
 }
 

@@ -151,6 +151,11 @@ int tiling_max_threads(int reg);
 
 cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+// FP64 stage and rates with the alternative stencil orders (stage_orders.cu)
+cudaError_t launch_step_fp64_order(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
+                                   const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+cudaError_t launch_rates_fp64_order(const Grid& g, const Ptr36& in, const MPtr36& out, const ewpt_params& p,
+                                    double Jex, double gam, cudaStream_t st);
 // DF64 form (stage_dd.cu): y, yn, xa, xb hold float pairs (hi, lo).
 cudaError_t launch_step_dd(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                            const ewpt_params& p, double Jex, double gam, cudaStream_t st);

@@ -31,7 +31,7 @@ class EwptParams(C.Structure):
                 ("lam", C.c_double), ("vev", C.c_double), ("theta_w", C.c_double),
                 ("beta_w", C.c_double), ("beta_y", C.c_double), ("gamma_inp", C.c_double),
                 ("mH", C.c_double), ("t_sat", C.c_double),
-                ("thermal_init", C.c_int32), ("device", C.c_int32)]
+                ("thermal_init", C.c_int32), ("device", C.c_int32), ("stencil_order", C.c_int32)]
 
 
 class EwptError(RuntimeError):

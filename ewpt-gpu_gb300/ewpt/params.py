@@ -46,6 +46,7 @@ class Params:
     precision: int = _lib.FP64
     shape: tuple | None = None  # (nx, ny, nz); defaults to (N, N, N)
     device: int = 0
+    stencil_order: int = 6  # 2, 6, 8, 10 or 12 (diff_scheme.jl modules); != 6 needs FP64
 
     @classmethod
     def from_args(cls, args: list[str], **over) -> "Params":
@@ -87,7 +88,8 @@ class Params:
         nx, ny, nz = self.dims
         return _lib.EwptParams(nx, ny, nz, int(self.precision), self.dx, self.dt, self.gw, self.gy, self.gp2,
                                self.lam, self.vev, self.theta_w, self.beta_w, self.beta_y, self.gamma_inp,
-                               self.mH, self.t_sat, int(bool(self.thermal_init)), int(self.device))
+                               self.mH, self.t_sat, int(bool(self.thermal_init)), int(self.device),
+                               int(self.stencil_order))
 
 
 def baseline_couplings(**over) -> Params:

@@ -21,13 +21,15 @@ struct Params
     beta_w::Float64; beta_y::Float64; gamma_inp::Float64
     mH::Float64; t_sat::Float64
     thermal_init::Int32; device::Int32
+    stencil_order::Int32   # 6, or 2/8/10/12: the diff_scheme.jl module `using`d by main_rk4.jl:33-35
 end
 
 const FP64 = Int32(0)
 const FP32 = Int32(1)
+const DF64 = Int32(2)
 
 """Params from the reference's 12 positional ARGS (parameters.jl:14-55)."""
-function Params(args::Vector{String}; precision=FP64, thermal_init=false, device=0)
+function Params(args::Vector{String}; precision=FP64, thermal_init=false, device=0, stencil_order=6)
     N = parse(Int32, args[6])
     dx = parse(Float64, args[4])
     dt = dx / parse(Float64, args[5])
@@ -37,7 +39,7 @@ function Params(args::Vector{String}; precision=FP64, thermal_init=false, device
     vev = 1.0
     Params(N, N, N, precision, dx, dt, gw, gw * tan(θ), parse(Float64, args[7]), lambda, vev, θ,
            parse(Float64, args[11]), parse(Float64, args[10]), parse(Float64, args[1]),
-           2.0 * sqrt(lambda) * vev, 2.0, Int32(thermal_init), Int32(device))
+           2.0 * sqrt(lambda) * vev, 2.0, Int32(thermal_init), Int32(device), Int32(stencil_order))
 end
 
 check(rc, ctx=C_NULL) = rc == 0 ? nothing :

@@ -68,6 +68,10 @@ typedef struct ewpt_params {
     double mH, t_sat;     /* J_ext/damp schedule, parameters.jl:24,40 */
     int32_t thermal_init; /* 1: apply J_ext/damp schedule (main_rk4.jl:5154-5172) */
     int32_t device;       /* CUDA device ordinal */
+    int32_t stencil_order;/* central-difference order of every stencil: 6 (default; 0 means 6) or
+                             2, 8, 10, 12 -- the modules of diff_scheme.jl:370-1438 that the
+                             driver selects with `using` (main_rk4.jl:33-35).  Orders other than 6
+                             need the FP64 form; every axis needs >= order + 1 sites. */
 } ewpt_params;
 
 typedef struct ewpt_ctx ewpt_ctx;

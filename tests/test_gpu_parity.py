@@ -32,7 +32,8 @@ def rel_err(a, b):
 
 
 def oparams(p: ewpt.Params):
-    return orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
+    return orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w,
+                      order=p.stencil_order)
 
 
 def golden(golden_dir, name):
@@ -372,3 +373,62 @@ def test_driver_energy_table_matches_oracle(tmp_path):
     ref = np.array(rows)
     np.testing.assert_allclose(res["energies"], ref[:, :13], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(res["total"], ref[:, 13], rtol=1e-9)
+
+
+# ------------------------------------------------------------ stencil orders
+@pytest.mark.parametrize("order", [8, 10, 12])
+def test_alternative_order_rates_match_golden(golden_dir, order):
+    """ewpt_rk4_rates with stencil_order 8/10/12 against rk4_step! run with
+    the reference's own 8th/10th/12th-order modules (14^3, beta, Jex, gamma)."""
+    import torch
+
+    g = golden(golden_dir, "orders")
+    p = params_from_golden(dict(g, dt=0.01), stencil_order=order)
+    yin = torch.tensor(g["y0"], device="cuda:0", dtype=torch.float64).contiguous()
+    out = torch.zeros_like(yin)
+    ewpt.rk4_rates_device(p, [yin[a].data_ptr() for a in range(36)], [out[a].data_ptr() for a in range(36)],
+                          float(g["Jex"]), float(g["gam"]), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rel_err(out.cpu().numpy(), g[f"rates_{order}"]) < 1e-12
+
+
+def test_second_order_rates_match_oracle(golden_dir):
+    """stencil_order 2 is the periodic 2nd-order stencil everywhere (the
+    reference's module misses the planes i = 2 and N-1; see the oracle tests)."""
+    import torch
+
+    g = golden(golden_dir, "orders")
+    p = params_from_golden(dict(g, dt=0.01), stencil_order=2)
+    yin = torch.tensor(g["y0"], device="cuda:0", dtype=torch.float64).contiguous()
+    out = torch.zeros_like(yin)
+    ewpt.rk4_rates_device(p, [yin[a].data_ptr() for a in range(36)], [out[a].data_ptr() for a in range(36)],
+                          float(g["Jex"]), float(g["gam"]), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    ref = orc.rates(oparams(p), g["y0"], float(g["Jex"]), float(g["gam"]))
+    assert rel_err(out.cpu().numpy(), ref) < 1e-12
+
+
+@pytest.mark.parametrize("order", [2, 8, 10, 12])
+def test_alternative_order_20_steps_and_diagnostics_vs_oracle(order):
+    shape = (16, 18, 14)
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.3, dt=0.02, beta_w=0.3, beta_y=0.2,
+                                stencil_order=order)
+    y0 = perturbed_bubbles(shape, p.dx, 3, seed=17)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        lat.step(20, Jex=0.02, gamma=0.01)
+        y = lat.get_state()
+        d = lat.diagnostics()
+    yo = orc.rk4_step(oparams(p), y0, p.dt, 0.02, 0.01, nsteps=20)
+    assert rel_err(y, yo) < 1e-11
+    do = orc.diagnostics(oparams(p), yo)
+    np.testing.assert_allclose(d[:14], do[:14], rtol=1e-9, atol=1e-12)
+
+
+def test_alternative_orders_rejected_where_not_offered():
+    with pytest.raises(ewpt.EwptError):
+        ewpt.Lattice(ewpt.baseline_couplings(shape=(16, 16, 16), N=16, precision=ewpt.FP32, stencil_order=8))
+    with pytest.raises(ewpt.EwptError):
+        ewpt.Lattice(ewpt.baseline_couplings(shape=(12, 16, 16), N=12, stencil_order=12))  # nx < 13
+    with pytest.raises(ewpt.EwptError):
+        ewpt.Lattice(ewpt.baseline_couplings(shape=(16, 16, 16), N=16, stencil_order=4))

@@ -2,9 +2,10 @@
 // width -> n_out, GELU, FP32 accumulate) trained on the GPU with hand-written
 // tensor-core forward/backward kernels and AdamW.
 //
-// GEMMs run on the tensor cores through mma.sync.m16n8k16 (bf16 x bf16 ->
-// f32): every product of the forward pass (X W^T), the weight gradients
-// (dZ^T A) and the input gradients (dZ W).  Weights are held in FP32 (the
+// GEMMs run on the 5th-generation tensor cores (tcgen05.mma kind::f16,
+// BF16 x BF16 -> FP32 accumulated in tensor memory; k_gemm_tc): every
+// product of the forward pass (X W^T), the weight gradients (dZ^T A) and the
+// input gradients (dZ W).  Weights are held in FP32 (the
 // optimizer's master copy) and in BF16 (the GEMM operand); activations and
 // gradients enter the GEMMs as BF16, pre-activations and accumulations stay
 // FP32.  This network has no counterpart in the reference: it maps early-time
@@ -25,14 +26,6 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-__device__ __forceinline__ void mma_bf16_16816(float* d, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 struct GemmArgs {
     const __nv_bfloat16* A;
     const __nv_bfloat16* B;
@@ -50,31 +43,141 @@ __device__ __forceinline__ __nv_bfloat16 ldB(const GemmArgs& g, int k, int n) {
     return g.transB ? g.B[(int64_t)n * g.ldb + k] : g.B[(int64_t)k * g.ldb + n];
 }
 
-// C[M x N] = op(A)[M x K] * op(B)[K x N].  Block of 4 warps = 32 x 16 tile,
-// each warp one m16n8 tile, K in steps of 16 (fragments per the PTX layout
-// of m16n8k16 .row.col: groupID = lane/4, tig = lane%4).
-__global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gid = lane >> 2, tig = lane & 3;
-    const int m0 = blockIdx.y * 32 + (warp >> 1) * 16;
-    const int n0 = blockIdx.x * 16 + (warp & 1) * 8;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k0 = 0; k0 < g.K; k0 += 16) {
-        uint32_t a[4], b[2];
-        const int kc = k0 + 2 * tig;
-        a[0] = pack_bf16(ldA(g, m0 + gid, kc), ldA(g, m0 + gid, kc + 1));
-        a[1] = pack_bf16(ldA(g, m0 + gid + 8, kc), ldA(g, m0 + gid + 8, kc + 1));
-        a[2] = pack_bf16(ldA(g, m0 + gid, kc + 8), ldA(g, m0 + gid, kc + 9));
-        a[3] = pack_bf16(ldA(g, m0 + gid + 8, kc + 8), ldA(g, m0 + gid + 8, kc + 9));
-        b[0] = pack_bf16(ldB(g, kc, n0 + gid), ldB(g, kc + 1, n0 + gid));
-        b[1] = pack_bf16(ldB(g, kc + 8, n0 + gid), ldB(g, kc + 9, n0 + gid));
-        mma_bf16_16816(acc, a, b);
+// ---------------------------------------------------------------- tcgen05
+// C[M x N] = op(A) op(B) on the 5th-generation tensor cores: one CTA of 4
+// warps per 128 x 64 tile of C, the FP32 accumulator in tensor memory (64
+// TMEM columns), K in slabs of 64.  Per slab the 128 threads gather op(A)
+// (128 x 64) and op(B)^T (64 x 64) as BF16 into shared memory in the
+// canonical K-major layout without swizzle -- 8-row x 16-byte core matrices,
+// adjacent along K 128 bytes apart (LBO), 8-row groups 1024 bytes apart
+// (SBO) -- (zero outside the matrices, any transposition done by the
+// gather), then one thread issues four tcgen05.mma (M 128, N 64, K 16) and
+// commits them to an mbarrier that every thread waits on before the slab is
+// overwritten.  Finally each warp reads its 32 TMEM lanes (rows) with
+// tcgen05.ld and writes C.  Every wait is bounded; a wait that runs out sets
+// g_tc_err and the kernel skips the remaining tensor-core work.
+constexpr int TC_M = 128, TC_N = 64, TC_K = 64;
+__device__ int g_tc_err = 0;
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, LBO, SBO (bytes), version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+    for (long it = 0; it < (1L << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
     }
-    const int r0 = m0 + gid, c0 = n0 + 2 * tig;
-    if (r0 < g.M && c0 < g.N) g.C[(int64_t)r0 * g.ldc + c0] = acc[0];
-    if (r0 < g.M && c0 + 1 < g.N) g.C[(int64_t)r0 * g.ldc + c0 + 1] = acc[1];
-    if (r0 + 8 < g.M && c0 < g.N) g.C[(int64_t)(r0 + 8) * g.ldc + c0] = acc[2];
-    if (r0 + 8 < g.M && c0 + 1 < g.N) g.C[(int64_t)(r0 + 8) * g.ldc + c0 + 1] = acc[3];
+    return false;
+}
+
+__global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
+    __shared__ __align__(1024) uint8_t sa[TC_M * TC_K * 2];  // 16 KB
+    __shared__ __align__(1024) uint8_t sb[TC_N * TC_K * 2];  // 8 KB
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * TC_N;
+    const uint32_t ubar = tc_smem(&bar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_base)),
+                     "r"(TC_N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ubar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+    const int nslab = (g.K + TC_K - 1) / TC_K;
+    for (int ks = 0; ks < nslab && ok; ++ks) {
+        const int k0 = ks * TC_K;
+        // gather op(A): row m = tid, 8 chunks of 8 K-elements (one core-matrix row each)
+        for (int kc = 0; kc < TC_K / 8; ++kc) {
+            uint32_t w[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                w[e] = pack_bf16(ldA(g, m0 + tid, k0 + 8 * kc + 2 * e), ldA(g, m0 + tid, k0 + 8 * kc + 2 * e + 1));
+            const int off = ((tid >> 3) * (TC_K / 8) + kc) * 128 + (tid & 7) * 16;
+            *reinterpret_cast<uint4*>(sa + off) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        // gather op(B)^T: row n, 8 chunks along K; 64 rows x 8 chunks over 128 threads
+        for (int q = tid; q < TC_N * (TC_K / 8); q += 128) {
+            const int n = q >> 3, kc = q & 7;
+            uint32_t w[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                w[e] = pack_bf16(ldB(g, k0 + 8 * kc + 2 * e, n0 + n), ldB(g, k0 + 8 * kc + 2 * e + 1, n0 + n));
+            const int off = ((n >> 3) * (TC_K / 8) + kc) * 128 + (n & 7) * 16;
+            *reinterpret_cast<uint4*>(sb + off) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t abase = tc_smem(sa), bbase = tc_smem(sb);
+#pragma unroll
+            for (int kk = 0; kk < TC_K / 16; ++kk) {
+                // K = 16 is two core matrices along K: advance 2 x LBO
+                const uint64_t ad = tc_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
+                const uint64_t bd = tc_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
+                const uint32_t acc = (ks > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(tc_idesc(TC_M, TC_N)), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(ubar)
+                         : "memory");
+        }
+        if (!tc_wait(ubar, ks & 1)) {
+            ok = false;
+            atomicExch(&g_tc_err, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < TC_N; c0 += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < g.M)
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                    if (n0 + c0 + e < g.N) g.C[(int64_t)row * g.ldc + n0 + c0 + e] = __uint_as_float(r[e]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
 }
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
@@ -186,7 +289,16 @@ int mlp_fail(ewpt_mlp* n, int code, const char* msg) {
 }
 
 int mlp_cuda(ewpt_mlp* n, cudaError_t e, const char* what) {
-    if (e == cudaSuccess) return EWPT_OK;
+    if (e == cudaSuccess) {
+        // a bounded tensor-core wait that ran out (k_gemm_tc) invalidates the results
+        int h = 0;
+        if (cudaMemcpyFromSymbol(&h, g_tc_err, sizeof h) == cudaSuccess && h) {
+            const int z = 0;
+            cudaMemcpyToSymbol(g_tc_err, &z, sizeof z);
+            return mlp_fail(n, EWPT_ERR_TIMEOUT, "a tensor-core wait in the MLP GEMM ran out (results invalid)");
+        }
+        return EWPT_OK;
+    }
     std::string s = std::string(what) + ": " + cudaGetErrorString(e);
     return mlp_fail(n, e == cudaErrorMemoryAllocation ? EWPT_ERR_OOM : EWPT_ERR_CUDA, s.c_str());
 }
@@ -194,8 +306,8 @@ int mlp_cuda(ewpt_mlp* n, cudaError_t e, const char* what) {
 cudaError_t gemm(cudaStream_t st, const __nv_bfloat16* A, int lda, int transA, const __nv_bfloat16* B, int ldb,
                  int transB, float* C, int ldc, int M, int N, int K) {
     GemmArgs g{A, B, C, M, N, K, lda, ldb, ldc, transA, transB};
-    const dim3 gr((N + 15) / 16, (M + 31) / 32);
-    k_gemm_bf16<<<gr, 128, 0, st>>>(g);
+    const dim3 gr((N + TC_N - 1) / TC_N, (M + TC_M - 1) / TC_M);
+    k_gemm_tc<<<gr, 128, 0, st>>>(g);
     return cudaGetLastError();
 }
 

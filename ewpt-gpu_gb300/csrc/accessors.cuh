@@ -23,6 +23,14 @@ struct SrcBase {
     __device__ __forceinline__ const TL* arr(int a) const { return base + a * S; }
 };
 
+// [36][S] block with 36 S < 2^31: 32-bit array offsets
+template <typename TL>
+struct SrcBase32 {
+    const TL* base;
+    int S;
+    __device__ __forceinline__ const TL* arr(int a) const { return base + a * S; }
+};
+
 // One site per thread; TL = stored type, T = arithmetic type.
 template <typename TL, typename T, class Src>
 struct SiteAcc {

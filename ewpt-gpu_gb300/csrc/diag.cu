@@ -262,8 +262,9 @@ __global__ void k_diag_final(const double* __restrict__ part, int nb, double* __
     }
 }
 
-// Writes one real field per component for the spectra: which = 0 -> B
-// (compute_Bx/By/Bz!), 1 -> B_2 (compute_B_2_*!), 2 -> Higgs phi_1..4.
+// Writes one real field per component: which = 0 -> B (compute_Bx/By/Bz!),
+// 1 -> B_2 (compute_B_2_*!), 2 -> Higgs phi_1..4, 3 -> the seven energy
+// densities (compute_PE! .. compute_MEY!).
 template <int R>
 __global__ void __launch_bounds__(DT) k_fields(Grid g, const double* __restrict__ y, DiagCoef kc, int which,
                                                double* __restrict__ f) {
@@ -281,6 +282,12 @@ __global__ void __launch_bounds__(DT) k_fields(Grid g, const double* __restrict_
         make_dacc<R>(g, y, kc, i, j, k, A);
         SiteDiag o;
         site_diag(A, kc, o);
+        if (which == 3) {
+            const double d[7] = {o.pe, o.ke, o.ge, o.eew, o.mew, o.eey, o.mey};
+#pragma unroll
+            for (int q = 0; q < 7; ++q) f[q * g.S + c] = d[q];
+            continue;
+        }
         f[c] = which == 0 ? o.bx : o.b2x;
         f[g.S + c] = which == 0 ? o.by : o.b2y;
         f[2 * g.S + c] = which == 0 ? o.bz : o.b2z;
@@ -433,6 +440,40 @@ cudaError_t launch_fields(const Grid& g, const ewpt_params& p, const double* y, 
         default: k_fields<3><<<gr, bl, 0, st>>>(g, y, kc, which, f);
     }
     return cudaGetLastError();
+}
+
+extern "C" int32_t ewpt_field_components(int32_t field) {
+    switch (field) {
+        case EWPT_FIELD_B:
+        case EWPT_FIELD_B2: return 3;
+        case EWPT_FIELD_HIGGS: return 4;
+        case EWPT_FIELD_DENSITY: return 7;
+        default: return -1;
+    }
+}
+
+extern "C" int ewpt_fields(ewpt_ctx* c, int32_t field, double* out, int32_t on_device) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    const int ncomp = ewpt_field_components(field);
+    if (ncomp < 0) return ewpt_fail(c, EWPT_ERR_ARG, "field %d unknown", field);
+    if (!out) return ewpt_fail(c, EWPT_ERR_ARG, "out is NULL");
+    cudaSetDevice(c->p.device);
+    const double* y;
+    int rc = ewpt_state64(c, &y);
+    if (rc) return rc;
+    const size_t bytes = (size_t)ncomp * c->g.S * 8;
+    double* f = out;
+    cudaError_t e = cudaSuccess;
+    if (!on_device) e = cudaMallocAsync(&f, bytes, c->st);
+    const int which = field == EWPT_FIELD_B ? 0 : field == EWPT_FIELD_B2 ? 1 : field == EWPT_FIELD_HIGGS ? 2 : 3;
+    if (e == cudaSuccess) e = launch_fields(c->g, c->p, y, which, f, c->st);
+    if (!on_device && f != out) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, f, bytes, cudaMemcpyDeviceToHost, c->st);
+        const cudaError_t ef = cudaFreeAsync(f, c->st);
+        if (e == cudaSuccess) e = ef;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    }
+    return ewpt_cuda_check(c, e, "fields");
 }
 
 extern "C" int ewpt_diagnostics(ewpt_ctx* c, double out[EWPT_NDIAG]) {

@@ -57,7 +57,7 @@ __device__ __forceinline__ int find_member(const EnsMember* __restrict__ tab, in
 
 template <int STAGE, typename T>
 struct EnsSink {
-    int64_t S, c;
+    int S, c;  // 36 S < 2^31 (checked at creation): 32-bit offsets within a member
     float* kacc;
     float* yhi;
     float* ylo;
@@ -78,7 +78,7 @@ struct EnsSink {
             *p = v;
     }
     __device__ __forceinline__ void operator()(int a, T r) const {
-        const int64_t q = a * S + c;
+        const int q = a * S + c;
         if (STAGE == 1) {
             wr(kacc + q, r);
             wr(xn + q, T(rd(xin + q) + h * r));
@@ -119,19 +119,19 @@ __global__ void __launch_bounds__(128, 1) k_ens_stage(const EnsMember* __restric
         const int j = ty * (int)blockDim.y + (int)threadIdx.y;
         if (i >= M.nx || j >= M.ny) continue;
         const PhysCoef<T> pc = widen<T>(M.pc);
-        EnsSink<STAGE, T> out{M.S,          0,
+        EnsSink<STAGE, T> out{(int)M.S,     0,
                               b.kacc + M.off, b.yhi + M.off,
                               b.ylo + M.off, xn ? xn + M.off : nullptr,
                               T(STAGE == 3 ? M.h1 : M.h2), T(M.w6),
                               xin + M.off};
         if constexpr (PAIR) {
-            PairAcc<SrcBase<float>> A{{xin + M.off, M.S}};
+            PairAcc<SrcBase32<float>> A{{xin + M.off, (int)M.S}};
             A.place(i, j, k, M.nx, M.ny, M.nz);
             A.s = pair_stencil(M.sc);
             out.c = A.c;
             site_rates<f2, BETA>(A, pc, out);
         } else {
-            SiteAcc<float, float, SrcBase<float>> A{{xin + M.off, M.S}};
+            SiteAcc<float, float, SrcBase32<float>> A{{xin + M.off, (int)M.S}};
             A.place(i, j, k, M.nx, M.ny, M.nz);
             A.s = M.sc;
             out.c = A.c;
@@ -248,6 +248,9 @@ int ewpt_ensemble_create(int32_t n, const ewpt_params* members, ewpt_ens** out) 
         if (rc) return rc;
         if (members[m].precision != EWPT_FP32)
             return ewpt_fail(nullptr, EWPT_ERR_ARG, "ensemble members use the FP32 form (member %d)", m);
+        if (36 * (int64_t)members[m].nx * members[m].ny * members[m].nz >= ((int64_t)1 << 31))
+            return ewpt_fail(nullptr, EWPT_ERR_ARG,
+                             "ensemble members need 36 nx ny nz < 2^31 (member %d); evolve larger lattices alone", m);
         if (members[m].device != members[0].device)
             return ewpt_fail(nullptr, EWPT_ERR_ARG, "all members must be on one device");
     }

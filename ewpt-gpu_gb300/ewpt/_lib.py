@@ -19,7 +19,7 @@ NDIAG = 20
 
 OK, ERR_ARG, ERR_CUDA, ERR_CUFFT, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_STATE = range(8)
 FP64, FP32, DF64 = 0, 1, 2
-FIELD_B, FIELD_B2, FIELD_HIGGS = 0, 1, 2
+FIELD_B, FIELD_B2, FIELD_HIGGS, FIELD_DENSITY = 0, 1, 2, 3
 BUBBLE_REFERENCE, BUBBLE_TANH = 0, 1
 SPEC_LOG, SPEC_UNIQUE = 0, 1
 
@@ -67,6 +67,9 @@ def _sig(L):
     L.ewpt_rk4_rates.argtypes = [P, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
     L.ewpt_diagnostics.argtypes = [V, DP]
     L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
+    L.ewpt_field_components.argtypes = [C.c_int32]
+    L.ewpt_field_components.restype = C.c_int32
+    L.ewpt_fields.argtypes = [V, C.c_int32, DP, C.c_int32]
     L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_kc_bin_nums.restype = C.c_int64
     L.ewpt_diagnostics_noalloc.argtypes = [P, C.c_void_p, DP, C.c_void_p]

@@ -18,7 +18,9 @@ from .params import Params
 DIAG_NAMES = ["PE", "KE", "GE", "EEW", "MEW", "EEY", "MEY", "EB", "EB2", "min_phi", "zero", "mean_phi",
               "helicity", "total", "gauss_W", "gauss_W_max", "gauss_Y", "gauss_Y_max", "aux_W", "aux_Y"]
 
-FIELDS = {"B": _lib.FIELD_B, "B2": _lib.FIELD_B2, "higgs": _lib.FIELD_HIGGS}
+FIELDS = {"B": _lib.FIELD_B, "B2": _lib.FIELD_B2, "higgs": _lib.FIELD_HIGGS, "density": _lib.FIELD_DENSITY}
+# components of fields("density"): the E_t of compute_PE! .. compute_MEY!
+DENSITY_NAMES = ["PE", "KE", "GE", "EEW", "MEW", "EEY", "MEY"]
 MODES = {"log": _lib.SPEC_LOG, "unique": _lib.SPEC_UNIQUE}
 
 
@@ -118,6 +120,15 @@ class Lattice:
         self._chk(rc)
         return out
 
+    def fields(self, field: str = "B") -> np.ndarray:
+        """Per-site fields (ewpt_fields): (ncomp, S) float64, each row in the
+        state's order; julia_array(row, dims) gives the [x, y, z] view."""
+        f = FIELDS[field]
+        n = int(self.L.ewpt_field_components(f))
+        out = np.empty((n, self.params.sites))
+        self._chk(self.L.ewpt_fields(self.h, f, out.ctypes.data_as(_lib.DP), 0))
+        return out
+
     def spectrum(self, field: str = "B", mode: str = "log", nbins: int = 40) -> dict:
         k, s, c, m = (np.zeros(nbins) for _ in range(4))
         nout = C.c_int32(0)
@@ -139,3 +150,9 @@ def rk4_rates_device(params: Params, in_ptrs, out_ptrs, Jex: float = 0.0, gamma:
 
 def kc_bin_nums(cx: int, cy: int, cz: int) -> int:
     return int(_lib.load().ewpt_kc_bin_nums(cx, cy, cz))
+
+
+def julia_array(row: np.ndarray, dims) -> np.ndarray:
+    """View of one [S] state-order array as the reference's Array{T,3}:
+    a[i, j, k] with i (x) fastest in memory (Fortran order)."""
+    return np.asarray(row).reshape(tuple(dims), order="F")

@@ -37,6 +37,7 @@ class Params:
     T: float = 0.0
     nte: int = 1000
     nsnaps: int = 10
+    nsnaps_fft: int = 50
     no_bubbles: int = 10
     base_seed: int = 123456
     mH: float = 2.0 * math.sqrt(0.129)
@@ -74,6 +75,12 @@ class Params:
     @property
     def dsnaps(self) -> int:
         return max(1, int(math.floor(self.nte / self.nsnaps)))
+
+    @property
+    def dsnaps_fft(self) -> int:
+        """Steps between 3D B-FFT dumps: floor(nte / nsnaps_fft), nsnaps_fft = 50
+        (parameters.jl:46-48); at least 1."""
+        return max(1, int(math.floor(self.nte / self.nsnaps_fft)))
 
     @property
     def bub_diam(self) -> int:

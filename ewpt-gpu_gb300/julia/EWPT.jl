@@ -93,6 +93,19 @@ function spectrum(L::Lattice; field=0, mode=0, nbins=40)
     (k=k[1:n[]], sum=s[1:n[]], count=c[1:n[]], mean=m[1:n[]])
 end
 
+"""Per-site fields as Julia arrays (nx, ny, nz, ncomp): field 0 = B_x,B_y,B_z
+(the E_t of compute_Bx/By/Bz!), 1 = B_2, 2 = phi_1..phi_4, 3 = the energy
+densities PE, KE, GE, EEW, MEW, EEY, MEY (compute_PE! .. compute_MEY!).
+`fields(L; field=0)[:, :, :, 1]` is the reference's B_x E_t, so
+`fft(fields(L)[:, :, :, 1])` is its B_x_fft (main_rk4.jl:6579-6580)."""
+function fields(L::Lattice; field=0)
+    n = ccall((:ewpt_field_components, libewpt), Int32, (Int32,), field)
+    n > 0 || error("unknown field $field")
+    out = zeros(Float64, L.p.nx, L.p.ny, L.p.nz, n)
+    check(ccall((:ewpt_fields, libewpt), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Int32), L.h, field, out, 0), L.h)
+    out
+end
+
 """Drop-in for `@cuda rk4_step!(...)`: `inputs` = 20 fields then 16 momenta,
 `outputs` = 20 k then 16 kt, all CuArray{Float64,3} device pointers (pass
 `pointer.(arrays)` of CuArrays as UInt64 / Ptr{Float64})."""

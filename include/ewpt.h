@@ -149,7 +149,7 @@ int ewpt_rk4_rates(const ewpt_params* p, const double* const in[EWPT_NARR],
  * column is NaN/Inf. */
 int ewpt_diagnostics(ewpt_ctx* ctx, double out[EWPT_NDIAG]);
 
-enum ewpt_field { EWPT_FIELD_B = 0, EWPT_FIELD_B2 = 1, EWPT_FIELD_HIGGS = 2 };
+enum ewpt_field { EWPT_FIELD_B = 0, EWPT_FIELD_B2 = 1, EWPT_FIELD_HIGGS = 2, EWPT_FIELD_DENSITY = 3 };
 enum ewpt_spec_mode { EWPT_SPEC_LOG = 0, EWPT_SPEC_UNIQUE = 1 };
 
 /* Power spectrum of the current state (replaces fft(E_t) + convolve_1d,
@@ -167,6 +167,21 @@ enum ewpt_spec_mode { EWPT_SPEC_LOG = 0, EWPT_SPEC_UNIQUE = 1 };
  * NULL) = bins written.  Synchronous. */
 int ewpt_spectrum(ewpt_ctx* ctx, int32_t field, int32_t mode, int32_t nbins, double* k, double* sum,
                   double* count, double* mean, int32_t* nbins_out);
+
+/* Per-site fields of the current state in FP64, one nx*ny*nz array per
+ * component in the state's order (x fastest: a Julia Array{Float64,3}):
+ *   EWPT_FIELD_B        3: B_x, B_y, B_z (the E_t of compute_Bx/By/Bz!)
+ *   EWPT_FIELD_B2       3: B_2 components (compute_B_2_x/y/z!)
+ *   EWPT_FIELD_HIGGS    4: phi_1..phi_4 as stored
+ *   EWPT_FIELD_DENSITY  7: energy densities PE, KE, GE, EEW, MEW, EEY, MEY
+ *                          (the E_t of compute_PE! .. compute_MEY!,
+ *                          main_rk4.jl:1334-2301; sum * dx^3 = the energy)
+ * The reference takes its y-slices (main_rk4.jl:6451-6560) and 3D B FFTs
+ * (:6579-6868) from these arrays.  out holds ewpt_field_components(field)
+ * * nx*ny*nz doubles, on the host (on_device = 0) or the device.  Synchronous
+ * for host output. */
+int32_t ewpt_field_components(int32_t field);
+int ewpt_fields(ewpt_ctx* ctx, int32_t field, double* out, int32_t on_device);
 
 /* Number of distinct |K| on a cx*cy*cz index lattice (Kc_bin_nums,
  * spec_routines.jl:32-43), -1 on bad input. */

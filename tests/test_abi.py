@@ -69,6 +69,44 @@ def test_kc_bin_nums_host(L):
     assert L.ewpt_kc_bin_nums(0, 1, 1) == -1
 
 
+def test_field_components_host(L):
+    assert [L.ewpt_field_components(f) for f in range(4)] == [3, 3, 4, 7]
+    assert L.ewpt_field_components(4) == -1 and L.ewpt_field_components(-1) == -1
+    assert L.ewpt_fields(None, 0, None, 0) == _lib.ERR_ARG
+
+
+def test_h5_layout_reverses_julia_axes():
+    """HDF5.jl writes a Julia array with reversed dimensions and the same
+    memory; the converter writes the transpose of each Julia-axes array."""
+    import numpy as np
+
+    from ewpt import h5convert
+
+    a = np.asfortranarray(np.arange(24.0).reshape(2, 3, 4))  # Julia A[x, y, z], column-major
+    h = h5convert.julia_layout(a)
+    assert h.shape == (4, 3, 2) and h.flags["C_CONTIGUOUS"]
+    assert np.shares_memory(h, a) or np.array_equal(h.ravel(), a.ravel(order="F"))
+    assert h[3, 2, 1] == a[1, 2, 3]
+    s = np.float64(0.25)
+    assert h5convert.julia_layout(s) == s
+
+
+def test_h5convert_writes_reference_datasets(tmp_path):
+    h5py = pytest.importorskip("h5py")
+    import numpy as np
+
+    from ewpt import h5convert
+
+    e = np.asfortranarray(np.random.default_rng(0).normal(size=(5, 13)))
+    np.savez(tmp_path / "data.npz", Nx=np.int64(8), energies=e)
+    np.savez(tmp_path / "3d-fft-data-0.npz", **{"3D_fft_x": np.asfortranarray(np.ones((4, 4, 4), complex))})
+    out = h5convert.convert_dir(str(tmp_path))
+    assert sorted(map(str, out)) == sorted([str(tmp_path / "data.h5"), str(tmp_path / "3d-fft-data-0.h5")])
+    with h5py.File(tmp_path / "data.h5") as f:
+        assert f["energies"].shape == (13, 5) and int(f["Nx"][()]) == 8
+        np.testing.assert_array_equal(f["energies"][()].T, e)
+
+
 def test_params_from_reference_args():
     p = ewpt.Params.from_args(["0.0", "10", "200", "0.25", "20", "64", "0.99", "20", "0.0", "0.0", "0.0", "1"])
     assert p.N == 64 and p.dt == 0.25 / 20 and p.dsnaps == 10 and p.base_seed == 123456

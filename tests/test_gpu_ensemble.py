@@ -78,3 +78,7 @@ def test_ensemble_rejects_bad_members():
     p = ewpt.baseline_couplings(N=16, precision=ewpt.FP64)
     with pytest.raises(ewpt.EwptError):
         ewpt.Ensemble([p])
+    # members index their [36][S] block with 32-bit offsets: 36 S < 2^31
+    big = ewpt.baseline_couplings(N=392, precision=ewpt.FP32)
+    with pytest.raises(ewpt.EwptError, match="2\\^31"):
+        ewpt.Ensemble([ewpt.baseline_couplings(N=16, precision=ewpt.FP32), big])

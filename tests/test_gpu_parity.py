@@ -375,6 +375,80 @@ def test_driver_energy_table_matches_oracle(tmp_path):
     np.testing.assert_allclose(res["total"], ref[:, 13], rtol=1e-9)
 
 
+@pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32, ewpt.DF64])
+def test_fields_match_oracle_densities(prec):
+    """ewpt_fields: the energy densities, B and B_2 per site equal the
+    oracle's site densities (the E_t arrays of compute_PE! .. compute_B_2_z!),
+    the Higgs field is the stored state, and the sums times dx^3 are the
+    diagnostics row."""
+    shape = (18, 16, 20)
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, precision=prec)
+    y0 = perturbed_bubbles(shape, p.dx, 3, seed=5, amp=0.2)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        y = lat.get_state()  # the state as this form holds it
+        dens, B, B2, H = (lat.fields(f) for f in ("density", "B", "B2", "higgs"))
+        row = lat.diagnostics()
+        with pytest.raises(ewpt.EwptError):
+            lat._chk(lat.L.ewpt_fields(lat.h, 9, B.ctypes.data_as(ewpt._lib.DP), 0))
+    den = orc.densities(oparams(p), y)
+    assert dens.shape == (7, p.sites) and B.shape == B2.shape == (3, p.sites) and H.shape == (4, p.sites)
+    assert rel_err(dens, den[:7]) < 1e-12
+    assert rel_err(B, den[7:10]) < 1e-12
+    assert rel_err(B2, den[10:13]) < 1e-12
+    np.testing.assert_array_equal(H, y[:4])
+    np.testing.assert_allclose(dens.sum(axis=1) * p.dx ** 3, row[:7], rtol=1e-11)
+    np.testing.assert_allclose(0.5 * (B ** 2).sum() * p.dx ** 3, row[7], rtol=1e-11)
+
+
+def test_driver_reference_outputs(tmp_path):
+    """ewpt.run writes the datasets of data.h5 and 3d-fft-data-<it>.h5 as
+    .npz: y_slices_snaps are the y = Ny/2 planes of the oracle's densities
+    and B sums times dx^3 (main_rk4.jl:5700-5960), and the FFT dump is
+    fft(E_t) of the oracle's B and B_2 over the Julia axes."""
+    from ewpt import run as drv
+    from ewpt.lattice import julia_array
+
+    args = ["0.0", "4", "20", "0.25", "10", "32", "0.99", "4", "0.0", "0.0", "0.0", "2"]
+    p = ewpt.Params.from_args(args, nsnaps_fft=2)
+    res = drv.run(p, out_dir=str(tmp_path), nshell=12, verbose=False, fft_dumps=True)
+    z = np.load(tmp_path / "data.npz")
+    for k in ("Nx", "gp2", "dx", "dt", "nte", "gamma", "T", "meff_sq", "t_sat_jex", "nsnaps", "dsnaps",
+              "no_bubbles", "bubble_locations", "Hoft_angles", "energies", "y_slices_snaps"):
+        assert k in z.files, k
+    nx, ny, nz = p.dims
+    assert z["energies"].shape == (5, 13) and z["y_slices_snaps"].shape == (5, 7, nx, nz)
+    assert z["bubble_locations"].shape == (4, 3) and z["Hoft_angles"].shape == (4, 3)
+    np.testing.assert_array_equal(z["energies"], res["energies"])
+    # snapshot 0 against the oracle's densities of the same IC
+    op = oparams(p)
+    y = np.zeros((36, p.sites))
+    for b in drv.reference_bubble_list(p):
+        orc.bubble_rmag(op, y, b[:3], b[3:], p.mH)
+    den = orc.densities(op, y)
+    vol = p.dx ** 3
+    j = ny // 2 - 1
+
+    def plane(q):
+        return julia_array(den[q], p.dims)[:, j, :] * vol
+
+    s0 = z["y_slices_snaps"][0]
+    scale = np.abs(s0).max()
+    for q, ref in enumerate([plane(0), plane(1), plane(2), plane(4) + plane(3) + plane(6) + plane(5),
+                             plane(7) + plane(8) + plane(9), plane(10) + plane(11) + plane(12)]):
+        assert np.abs(s0[q] - ref).max() <= 1e-11 * scale, q
+    assert not s0[6].any()
+    # FFT dumps at iteration 0 and every dsnaps_fft = 10 steps at snapshots (5, 10, 15, 20)
+    assert list(res["fft_dump_iterations"]) == [0, 10, 20]
+    f0 = np.load(tmp_path / "3d-fft-data-0.npz")
+    assert sorted(f0.files) == sorted(["3D_fft_x", "3D_fft_y", "3D_fft_z", "3D_fft_x2", "3D_fft_y2", "3D_fft_z2"])
+    for name, q in (("3D_fft_x", 7), ("3D_fft_z", 9), ("3D_fft_y2", 11)):
+        ref = np.fft.fftn(julia_array(den[q], p.dims))
+        assert f0[name].shape == (nx, ny, nz) and f0[name].dtype == np.complex128
+        assert np.abs(f0[name] - ref).max() <= 1e-10 * np.abs(ref).max(), name
+    assert (tmp_path / "3d-fft-data-20.npz").exists()
+
+
 # ------------------------------------------------------------ stencil orders
 @pytest.mark.parametrize("order", [8, 10, 12])
 def test_alternative_order_rates_match_golden(golden_dir, order):

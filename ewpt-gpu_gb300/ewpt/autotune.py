@@ -85,7 +85,8 @@ def sweep(p: Params, steps: int = 2, candidates=None) -> list:
             candidates += [t for t in TMA_CANDIDATES if ny % t[1] == 0 and nz % t[2] == 0]
     res = []
     with Lattice(p) as lat:
-        lat.set_state(ic.bubbles_tanh(p.dims, p.dx, 4, seed=0))
+        R, w = ic.tanh_profile_params(p.lam, p.vev)
+        lat.init_bubbles(ic.tanh_bubble_list(p.dims, p.dx, 4, seed=0), "tanh", R, w)  # device IC: no host state
         for t in candidates:
             try:
                 res.append((t, time_tiling(lat, t, steps)))

@@ -506,3 +506,32 @@ def test_alternative_orders_rejected_where_not_offered():
         ewpt.Lattice(ewpt.baseline_couplings(shape=(12, 16, 16), N=12, stencil_order=12))  # nx < 13
     with pytest.raises(ewpt.EwptError):
         ewpt.Lattice(ewpt.baseline_couplings(shape=(16, 16, 16), N=16, stencil_order=4))
+
+
+# ------------------------------------------------------------ largest lattice
+def test_largest_lattice_forms_agree():
+    """512^3 (36 S = 4.8e9 > 2^31 array elements; FP64 context 155 GB):
+    the same device bubble IC stepped twice by the FP64, DF64 and FP32 forms
+    gives the same snapshot row (DF64 to the FP64 bar, FP32 to its
+    round-off), so the 64-bit array offsets, the ghosted FP32 layout and the
+    autotuned launch shapes hold at the largest size the GPU takes."""
+    from ewpt import autotune
+
+    N = 512
+    rows = {}
+    for name, prec in (("fp64", ewpt.FP64), ("df64", ewpt.DF64), ("fp32", ewpt.FP32)):
+        p = ewpt.baseline_couplings(N=N, dx=0.25, dt=0.025, precision=prec)
+        R, w = ewpt.ic.tanh_profile_params(p.lam, p.vev)
+        # the sweep runs on its own scratch lattice: pick the shape first
+        tile = autotune.best_tiling(p, steps=1) if prec == ewpt.FP32 else None
+        with ewpt.Lattice(p) as lat:
+            lat.init_bubbles(ewpt.ic.tanh_bubble_list(p.dims, p.dx, 64, seed=3), "tanh", R, w)
+            if tile:
+                lat.set_tiling(*tile)
+            lat.step(2)
+            rows[name] = lat.diagnostics()
+    for r in rows.values():
+        assert np.isfinite(r).all()
+    cols = [0, 1, 2, 3, 4, 7, 11, 13]  # PE KE GE EEW MEW EB mean|phi| total
+    np.testing.assert_allclose(rows["df64"][cols], rows["fp64"][cols], rtol=1e-10)
+    np.testing.assert_allclose(rows["fp32"][cols], rows["fp64"][cols], rtol=1e-4)

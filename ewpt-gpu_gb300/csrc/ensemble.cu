@@ -55,15 +55,15 @@ __device__ __forceinline__ int find_member(const EnsMember* __restrict__ tab, in
     return lo;
 }
 
-// RK4 epilogue of one member site.  The five buffers come from the kernel's
-// parameter block (constant bank) and the member's offset from one register,
-// so no per-member pointer stays live across the physics.
 template <int STAGE, typename T>
 struct EnsSink {
-    const EnsBufs& b;
-    int64_t off;
     int S, c;  // 36 S < 2^31 (checked at creation): 32-bit offsets within a member
+    float* kacc;
+    float* yhi;
+    float* ylo;
+    float* xn;
     T h, w6;
+    const float* xin;  // stage input (for stage 1: y_hi)
 
     __device__ __forceinline__ static T rd(const float* p) {
         if constexpr (sizeof(T) == 8)
@@ -78,38 +78,21 @@ struct EnsSink {
             *p = v;
     }
     __device__ __forceinline__ void operator()(int a, T r) const {
-        const int64_t q = off + (a * S + c);
+        const int q = a * S + c;
         if (STAGE == 1) {
-            wr(b.kacc + q, r);
-            wr(b.xa + q, T(rd(b.yhi + q) + h * r));
+            wr(kacc + q, r);
+            wr(xn + q, T(rd(xin + q) + h * r));
         } else if (STAGE < 4) {
-            wr(b.kacc + q, T(rd(b.kacc + q) + T(2.f) * r));
-            wr((STAGE == 2 ? b.xb : b.xa) + q, T(rd(b.yhi + q) + h * r));
+            wr(kacc + q, T(rd(kacc + q) + T(2.f) * r));
+            wr(xn + q, T(rd(yhi + q) + h * r));
         } else {
-            const T s = rd(b.kacc + q) + r;
-            T hi = rd(b.yhi + q), lo = rd(b.ylo + q);
+            const T s = rd(kacc + q) + r;
+            T hi = rd(yhi + q), lo = rd(ylo + q);
             acc_hilo(hi, lo, T(w6 * s));
-            wr(b.yhi + q, hi);
-            wr(b.ylo + q, lo);
+            wr(yhi + q, hi);
+            wr(ylo + q, lo);
         }
     }
-};
-
-// Coefficients shared by every member (same couplings, dx, dt and drive):
-// passed as kernel parameters, i.e. constant-bank operands that take no
-// registers.  Pre-widened to the arithmetic type of the paired kernel.
-struct EnsShared {
-    PhysCoef<f2> pc;
-    StencilCoef<f2> sc;
-    f2 h2, h1, w6;
-};
-
-// Kernel modes: 0 = coefficients from the member table, registers at the
-// compiler's choice; 1 = shared coefficients, compiler's choice; 2 = shared
-// coefficients, at most 168 registers (12 warps per SM).
-template <int MODE>
-struct EnsBudget {
-    static constexpr int kThreads = 128, kMinBlocks = MODE == 2 ? 3 : 1;
 };
 
 template <typename T>
@@ -118,112 +101,50 @@ __device__ __forceinline__ PhysCoef<T> widen(const PhysCoef<float>& c) {
                        T(c.vev2), T(c.bW), T(c.bY), T(c.bW2), T(c.bY2), T(c.hJex), T(c.gam)};
 }
 
-template <int STAGE, bool BETA, bool PAIR, int MODE>
-__global__ void __launch_bounds__(EnsBudget<MODE>::kThreads, EnsBudget<MODE>::kMinBlocks)
-    k_ens_stage(const EnsMember* __restrict__ tab, int nmem, int64_t ntiles, const __grid_constant__ EnsBufs b,
-                const __grid_constant__ EnsShared sh) {
-    static_assert(PAIR || MODE == 0, "shared coefficients are offered with paired sites");
+template <int STAGE, bool BETA, bool PAIR>
+__global__ void __launch_bounds__(128, 1) k_ens_stage(const EnsMember* __restrict__ tab, int nmem, int64_t ntiles,
+                                                     EnsBufs b) {
     using T = typename std::conditional<PAIR, f2, float>::type;
     const float* xin = STAGE == 1 ? b.yhi : (STAGE == 3 ? b.xb : b.xa);
+    float* xn = STAGE == 1 ? b.xa : (STAGE == 2 ? b.xb : b.xa);
     for (int64_t w = blockIdx.x; w < ntiles; w += gridDim.x) {
         const int m = find_member(tab, nmem, w);
-        const EnsMember& M = tab[m];
-        const int nx = M.nx, ny = M.ny, nz = M.nz, tiles_x = M.tiles_x, tiles_y = M.tiles_y;
-        const int S = (int)M.S;
-        const int64_t off = M.off;
+        const EnsMember M = tab[m];
         int64_t t = w - M.tile0;
-        const int tx = (int)(t % tiles_x);
-        t /= tiles_x;
-        const int ty = (int)(t % tiles_y);
-        const int k = (int)(t / tiles_y);
+        const int tx = (int)(t % M.tiles_x);
+        t /= M.tiles_x;
+        const int ty = (int)(t % M.tiles_y);
+        const int k = (int)(t / M.tiles_y);
         const int i = (tx * (int)blockDim.x + (int)threadIdx.x) * (PAIR ? 2 : 1);
         const int j = ty * (int)blockDim.y + (int)threadIdx.y;
-        if (i >= nx || j >= ny) continue;
-        if constexpr (MODE == 0) {
-            const PhysCoef<T> pc = widen<T>(M.pc);
-            EnsSink<STAGE, T> out{b, off, S, 0, T(STAGE == 3 ? M.h1 : M.h2), T(M.w6)};
-            if constexpr (PAIR) {
-                PairAcc<SrcBase32<float>> A{{xin + off, S}};
-                A.place(i, j, k, nx, ny, nz);
-                A.s = pair_stencil(M.sc);
-                out.c = A.c;
-                site_rates<f2, BETA>(A, pc, out);
-            } else {
-                SiteAcc<float, float, SrcBase32<float>> A{{xin + off, S}};
-                A.place(i, j, k, nx, ny, nz);
-                A.s = M.sc;
-                out.c = A.c;
-                site_rates<float, BETA>(A, pc, out);
-            }
-        } else {
-            EnsSink<STAGE, f2> out{b, off, S, 0, STAGE == 3 ? sh.h1 : sh.h2, sh.w6};
-            PairAcc<SrcBase32<float>> A{{xin + off, S}};
-            A.place(i, j, k, nx, ny, nz);
-            A.s = sh.sc;
+        if (i >= M.nx || j >= M.ny) continue;
+        const PhysCoef<T> pc = widen<T>(M.pc);
+        EnsSink<STAGE, T> out{(int)M.S,     0,
+                              b.kacc + M.off, b.yhi + M.off,
+                              b.ylo + M.off, xn ? xn + M.off : nullptr,
+                              T(STAGE == 3 ? M.h1 : M.h2), T(M.w6),
+                              xin + M.off};
+        if constexpr (PAIR) {
+            PairAcc<SrcBase32<float>> A{{xin + M.off, (int)M.S}};
+            A.place(i, j, k, M.nx, M.ny, M.nz);
+            A.s = pair_stencil(M.sc);
             out.c = A.c;
-            site_rates<f2, BETA>(A, sh.pc, out);
+            site_rates<f2, BETA>(A, pc, out);
+        } else {
+            SiteAcc<float, float, SrcBase32<float>> A{{xin + M.off, (int)M.S}};
+            A.place(i, j, k, M.nx, M.ny, M.nz);
+            A.s = M.sc;
+            out.c = A.c;
+            site_rates<float, BETA>(A, pc, out);
         }
     }
 }
 
-template <bool BETA, bool PAIR, int MODE>
-int occupancy_blocks() {
+template <bool BETA, bool PAIR>
+void occupancy_blocks(int* nb) {
     int a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_ens_stage<2, BETA, PAIR, MODE>, 128, 0);
-    return a > 0 ? a : 1;
-}
-
-template <bool BETA, bool PAIR, int MODE>
-void launch_ens_step(const dim3& gr, const dim3& bl, cudaStream_t st, const EnsMember* tab, int n, int64_t ntiles,
-                     const EnsBufs& b, const EnsShared& sh) {
-    k_ens_stage<1, BETA, PAIR, MODE><<<gr, bl, 0, st>>>(tab, n, ntiles, b, sh);
-    k_ens_stage<2, BETA, PAIR, MODE><<<gr, bl, 0, st>>>(tab, n, ntiles, b, sh);
-    k_ens_stage<3, BETA, PAIR, MODE><<<gr, bl, 0, st>>>(tab, n, ntiles, b, sh);
-    k_ens_stage<4, BETA, PAIR, MODE><<<gr, bl, 0, st>>>(tab, n, ntiles, b, sh);
-}
-
-// Kernel variant (pair, mode): blocks per SM, and the four stage launches.
-template <bool BETA>
-int variant_blocks(bool pair, int mode) {
-    if (!pair) return occupancy_blocks<BETA, false, 0>();
-    if (mode == 2) return occupancy_blocks<BETA, true, 2>();
-    if (mode == 1) return occupancy_blocks<BETA, true, 1>();
-    return occupancy_blocks<BETA, true, 0>();
-}
-
-template <bool BETA>
-void variant_step(bool pair, int mode, const dim3& gr, const dim3& bl, cudaStream_t st, const EnsMember* tab, int n,
-                  int64_t ntiles, const EnsBufs& b, const EnsShared& sh) {
-    if (!pair)
-        launch_ens_step<BETA, false, 0>(gr, bl, st, tab, n, ntiles, b, sh);
-    else if (mode == 2)
-        launch_ens_step<BETA, true, 2>(gr, bl, st, tab, n, ntiles, b, sh);
-    else if (mode == 1)
-        launch_ens_step<BETA, true, 1>(gr, bl, st, tab, n, ntiles, b, sh);
-    else
-        launch_ens_step<BETA, true, 0>(gr, bl, st, tab, n, ntiles, b, sh);
-}
-
-// Whether every member has the same coefficients (couplings, dx, dt, drive).
-bool shared_coefficients(const std::vector<EnsMember>& tab) {
-    for (size_t m = 1; m < tab.size(); ++m)
-        if (std::memcmp(&tab[m].pc, &tab[0].pc, sizeof tab[0].pc) ||
-            std::memcmp(&tab[m].sc, &tab[0].sc, sizeof tab[0].sc) || tab[m].h2 != tab[0].h2 ||
-            tab[m].h1 != tab[0].h1 || tab[m].w6 != tab[0].w6)
-            return false;
-    return true;
-}
-
-EnsShared make_shared(const EnsMember& M) {
-    const PhysCoef<float>& c = M.pc;
-    EnsShared s;
-    s.pc = PhysCoef<f2>{f2(c.gw),   f2(c.gy),   f2(c.hgw), f2(c.hgy), f2(c.gp2), f2(c.omgp2), f2(c.lam2),
-                        f2(c.vev2), f2(c.bW),   f2(c.bY),  f2(c.bW2), f2(c.bY2), f2(c.hJex),  f2(c.gam)};
-    s.sc = pair_stencil(M.sc);
-    s.h2 = f2(M.h2);
-    s.h1 = f2(M.h1);
-    s.w6 = f2(M.w6);
-    return s;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_ens_stage<2, BETA, PAIR>, 128, 0);
+    *nb = a > 0 ? a : 1;
 }
 
 }  // namespace
@@ -238,9 +159,7 @@ struct ewpt_ens {
     EnsBufs b{};
     int64_t total = 0;  // sum of 36*S_m
     int64_t ntiles = 0;
-    int bx = 8, by = 8, pair = 0, reg = 0;  // 8x8 pair-threads: the fastest shape for mixed 48-160 members
-    int mode = 0;        // kernel mode in use (EnsBudget)
-    bool dirty = false;  // member coefficients changed since the graph was captured
+    int bx = 8, by = 8, pair = 0;  // 8x8 pair-threads: the fastest shape for mixed 48-160 members
     bool beta = false;
     int grid = 0;
     cudaGraph_t graph = nullptr;
@@ -278,30 +197,35 @@ static int ens_plan(ewpt_ens* e) {
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
     int rc = ens_cuda(e, ce, "ensemble table");
     if (rc) return rc;
-    int dev_sms = 0;
+    int dev_sms = 0, nb = 1;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, e->device);
-    const bool shared = e->pair && shared_coefficients(e->tab);
-    e->mode = shared ? (e->reg == 2 ? 2 : 1) : 0;
-    const EnsShared sh = make_shared(e->tab[0]);
-    const dim3 bl(e->bx, e->by);
-    const int nb = e->beta ? variant_blocks<true>(e->pair, e->mode) : variant_blocks<false>(e->pair, e->mode);
+    if (e->pair) {
+        if (e->beta) occupancy_blocks<true, true>(&nb); else occupancy_blocks<false, true>(&nb);
+    } else {
+        if (e->beta) occupancy_blocks<true, false>(&nb); else occupancy_blocks<false, false>(&nb);
+    }
     const int64_t cap = (int64_t)dev_sms * nb * std::max(1, 128 / (e->bx * e->by));
     e->grid = (int)std::min<int64_t>(cap, e->ntiles);
     if (e->exec) cudaGraphExecDestroy(e->exec), e->exec = nullptr;
     if (e->graph) cudaGraphDestroy(e->graph), e->graph = nullptr;
     ce = cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
-        const dim3 gr(e->grid);
-        if (e->beta)
-            variant_step<true>(e->pair, e->mode, gr, bl, e->st, e->dtab, e->n, e->ntiles, e->b, sh);
-        else
-            variant_step<false>(e->pair, e->mode, gr, bl, e->st, e->dtab, e->n, e->ntiles, e->b, sh);
+        const dim3 gr(e->grid), bl(e->bx, e->by);
+#define EWPT_ENS_LAUNCH(BETA, PAIR)                                                                  \
+    k_ens_stage<1, BETA, PAIR><<<gr, bl, 0, e->st>>>(e->dtab, e->n, e->ntiles, e->b);                 \
+    k_ens_stage<2, BETA, PAIR><<<gr, bl, 0, e->st>>>(e->dtab, e->n, e->ntiles, e->b);                 \
+    k_ens_stage<3, BETA, PAIR><<<gr, bl, 0, e->st>>>(e->dtab, e->n, e->ntiles, e->b);                 \
+    k_ens_stage<4, BETA, PAIR><<<gr, bl, 0, e->st>>>(e->dtab, e->n, e->ntiles, e->b);
+        if (e->beta && e->pair) { EWPT_ENS_LAUNCH(true, true) }
+        else if (e->beta) { EWPT_ENS_LAUNCH(true, false) }
+        else if (e->pair) { EWPT_ENS_LAUNCH(false, true) }
+        else { EWPT_ENS_LAUNCH(false, false) }
+#undef EWPT_ENS_LAUNCH
         cudaError_t le = cudaGetLastError();
         ce = cudaStreamEndCapture(e->st, &e->graph);
         if (ce == cudaSuccess) ce = le;
     }
     if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
-    if (ce == cudaSuccess) e->dirty = false;
     return ens_cuda(e, ce, "ensemble graph");
 }
 
@@ -470,19 +394,14 @@ int ewpt_ensemble_set_drive(ewpt_ens* e, int32_t m, double Jex, double gamma) {
     cudaSetDevice(e->device);
     cudaError_t ce = cudaMemcpyAsync(&e->dtab[m], &e->tab[m], sizeof(EnsMember), cudaMemcpyHostToDevice, e->st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
-    // the captured kernels may carry the shared coefficients as parameters:
-    // re-plan before the next step
-    e->dirty = true;
     return ens_cuda(e, ce, "ensemble set_drive");
 }
 
-int ewpt_ensemble_set_tiling(ewpt_ens* e, int32_t bx, int32_t by, int32_t reg, int32_t pair) {
+int ewpt_ensemble_set_tiling(ewpt_ens* e, int32_t bx, int32_t by, int32_t pair) {
     if (!e) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ensemble is NULL");
     if (bx < 1 || by < 1 || bx * by > 128 || (bx * by) % 32 != 0)
         return ens_fail(e, EWPT_ERR_ARG, "tile: need whole warps and at most 128 threads");
     if (pair != 0 && pair != 1) return ens_fail(e, EWPT_ERR_ARG, "pair must be 0 or 1");
-    if (reg != 0 && reg != 2) return ens_fail(e, EWPT_ERR_ARG, "reg must be 0 or 2");
-    if (reg == 2 && !pair) return ens_fail(e, EWPT_ERR_ARG, "reg 2 is offered with paired sites only");
     if (pair)
         for (const auto& p : e->mp)
             if (p.nx % 2) return ens_fail(e, EWPT_ERR_ARG, "paired sites need an even nx in every member");
@@ -491,7 +410,6 @@ int ewpt_ensemble_set_tiling(ewpt_ens* e, int32_t bx, int32_t by, int32_t reg, i
     e->bx = bx;
     e->by = by;
     e->pair = pair;
-    e->reg = reg;
     return ens_plan(e);
 }
 
@@ -499,10 +417,6 @@ int ewpt_ensemble_step(ewpt_ens* e, int32_t nsteps) {
     if (!e) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ensemble is NULL");
     if (nsteps < 0) return ens_fail(e, EWPT_ERR_ARG, "nsteps < 0");
     cudaSetDevice(e->device);
-    if (e->dirty && nsteps > 0) {
-        int rc = ens_plan(e);
-        if (rc) return rc;
-    }
     for (int s = 0; s < nsteps; ++s) {
         int rc = ens_cuda(e, cudaGraphLaunch(e->exec, e->st), "ensemble step");
         if (rc) return rc;

@@ -85,7 +85,7 @@ def _sig(L):
     L.ewpt_ensemble_set_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
     L.ewpt_ensemble_get_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
     L.ewpt_ensemble_set_drive.argtypes = [E, C.c_int32, C.c_double, C.c_double]
-    L.ewpt_ensemble_set_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_ensemble_set_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_ensemble_step.argtypes = [E, C.c_int32]
     L.ewpt_ensemble_sync.argtypes = [E]
     L.ewpt_ensemble_stream.argtypes = [E]

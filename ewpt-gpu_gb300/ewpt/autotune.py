@@ -115,15 +115,14 @@ def tune(lat: Lattice, steps: int = 2) -> tuple:
     return tile
 
 
-# (bx, by, pair, reg); narrow blocks (8 or 16 pair-threads = 16 or 32 sites
-# in x) waste fewer threads on members of 48 / 96 / 160 sites per row
-ENSEMBLE_CANDIDATES = [(16, 8, 1, 0), (8, 16, 1, 0), (8, 8, 1, 0), (16, 4, 1, 0), (8, 4, 1, 0), (32, 4, 1, 0),
-                       (32, 2, 1, 0), (16, 8, 1, 2), (8, 16, 1, 2), (8, 8, 1, 2), (16, 4, 1, 2), (32, 4, 1, 2),
-                       (32, 4, 0, 0), (16, 8, 0, 0)]
+# (bx, by, pair); narrow blocks (8 or 16 pair-threads = 16 or 32 sites in x)
+# waste fewer threads on members of 48 / 96 / 160 sites per row
+ENSEMBLE_CANDIDATES = [(8, 8, 1), (8, 16, 1), (16, 8, 1), (16, 4, 1), (8, 4, 1), (32, 4, 1), (32, 2, 1), (64, 2, 1),
+                       (32, 4, 0), (16, 8, 0), (32, 2, 0)]
 
 
 def best_ensemble_tiling(members, steps: int = 2, use_cache: bool = True) -> tuple:
-    """Fastest (bx, by, pair, reg) for an ensemble of these members, timed on a
+    """Fastest (bx, by, pair) for an ensemble of these members, timed on a
     scratch ensemble (so no live state is touched) and cached by the member
     shapes, couplings switches and GPU name."""
     import hashlib
@@ -134,7 +133,7 @@ def best_ensemble_tiling(members, steps: int = 2, use_cache: bool = True) -> tup
 
     shapes = ",".join(f"{p.dims[0]}x{p.dims[1]}x{p.dims[2]}" for p in members)
     beta = int(any(p.beta_w != 0.0 or p.beta_y != 0.0 for p in members))
-    key = "ens2:" + hashlib.sha1(shapes.encode()).hexdigest()[:16] + f":b{beta}:{torch.cuda.get_device_name(0)}"
+    key = "ens:" + hashlib.sha1(shapes.encode()).hexdigest()[:16] + f":b{beta}:{torch.cuda.get_device_name(0)}"
     cache = _load_cache() if use_cache else {}
     if key in cache:
         return tuple(cache[key]["tile"])

@@ -74,10 +74,8 @@ class Ensemble:
     def set_drive(self, m: int, Jex: float, gamma: float):
         self._chk(self.L.ewpt_ensemble_set_drive(self.h, m, float(Jex), float(gamma)))
 
-    def set_tiling(self, bx: int, by: int, pair: int, reg: int = 0):
-        """bx*by threads per block, pair = two x-adjacent sites per thread,
-        reg = register budget (0 the compiler's choice, 2 at most 168)."""
-        self._chk(self.L.ewpt_ensemble_set_tiling(self.h, bx, by, reg, pair))
+    def set_tiling(self, bx: int, by: int, pair: int):
+        self._chk(self.L.ewpt_ensemble_set_tiling(self.h, bx, by, pair))
 
     def step(self, n: int = 1):
         self._chk(self.L.ewpt_ensemble_step(self.h, int(n)))

@@ -225,12 +225,9 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* ens, int32_t m, int32_t nb, const doubl
 /* constant Jex and gamma of member m for the following steps */
 int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
 /* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent
- * sites per thread (every member needs an even nx; default when possible),
- * reg = register budget (0: the compiler's choice; 2: at most 168 per
- * thread, with pair = 1).  When every member has the same couplings, dx, dt
- * and drive, the paired kernel takes them as launch parameters; otherwise it
- * reads them per member and reg 2 is not used.  Default 8x8, reg 0. */
-int ewpt_ensemble_set_tiling(ewpt_ens* ens, int32_t bx, int32_t by, int32_t reg, int32_t pair);
+ * sites per thread (every member needs an even nx; default when possible).
+ * Default 8x8 threads. */
+int ewpt_ensemble_set_tiling(ewpt_ens* ens, int32_t bx, int32_t by, int32_t pair);
 /* nsteps RK4 steps of every member, asynchronous on the ensemble's stream */
 int ewpt_ensemble_step(ewpt_ens* ens, int32_t nsteps);
 int ewpt_ensemble_sync(ewpt_ens* ens);

@@ -74,36 +74,6 @@ def test_members_match_single_lattices(pair):
     np.testing.assert_allclose(sp["mean"], sref["mean"], rtol=1e-5 if not pair else 1e-12)
 
 
-@pytest.mark.parametrize("reg", [0, 2])
-def test_shared_coefficient_modes_match_single_lattices(reg):
-    """Members with one parameter set run the kernel that takes the
-    coefficients as launch parameters (reg 0 or the 168-register budget); a
-    drive on one member switches to per-member coefficients before the next
-    step, the same drive on every member switches back.  Every member stays
-    bit-identical to a single paired FP32 context throughout."""
-    ps = [ewpt.baseline_couplings(shape=shp, N=shp[0], dx=0.25, dt=0.025, precision=ewpt.FP32) for shp in SHAPES]
-    ys = _states(ps)
-    with ewpt.Ensemble(ps) as ens:
-        ens.set_tiling(16, 8, 1, reg)
-        for m, y in enumerate(ys):
-            ens.set_state(m, y)
-        ens.step(3)
-        ens.set_drive(2, 0.04, 0.01)  # per-member coefficients
-        ens.step(3)
-        for m in range(len(ps)):  # one shared drive again
-            ens.set_drive(m, 0.03, 0.02)
-        ens.step(3)
-        got = [ens.get_state(m) for m in range(len(ps))]
-    for m, (p, y) in enumerate(zip(ps, ys)):
-        with ewpt.Lattice(p) as lat:
-            lat.set_state(y)
-            lat.set_tiling(32, 4, reg, 1)
-            lat.step(3, Jex=0.0, gamma=0.0)
-            lat.step(3, Jex=0.04 if m == 2 else 0.0, gamma=0.01 if m == 2 else 0.0)
-            lat.step(3, Jex=0.03, gamma=0.02)
-            np.testing.assert_array_equal(got[m], lat.get_state())
-
-
 def test_ensemble_rejects_bad_members():
     p = ewpt.baseline_couplings(N=16, precision=ewpt.FP64)
     with pytest.raises(ewpt.EwptError):
@@ -112,15 +82,3 @@ def test_ensemble_rejects_bad_members():
     big = ewpt.baseline_couplings(N=392, precision=ewpt.FP32)
     with pytest.raises(ewpt.EwptError, match="2\\^31"):
         ewpt.Ensemble([ewpt.baseline_couplings(N=16, precision=ewpt.FP32), big])
-
-
-def test_ensemble_rejects_bad_tiling():
-    ps = [ewpt.baseline_couplings(N=n, precision=ewpt.FP32) for n in (16, 20)]
-    with ewpt.Ensemble(ps) as ens:
-        # (bx, by, pair, reg): partial warp, > 128 threads, pair 2, reg 1, reg 2 without pairs
-        for t in [(8, 3, 1, 0), (32, 8, 1, 0), (32, 4, 2, 0), (32, 4, 1, 1), (32, 4, 0, 2)]:
-            with pytest.raises(ewpt.EwptError):
-                ens.set_tiling(*t)
-        ens.set_tiling(32, 4, 1, 2)
-        ens.step(1)
-        ens.sync()

@@ -82,3 +82,15 @@ def test_ensemble_rejects_bad_members():
     big = ewpt.baseline_couplings(N=392, precision=ewpt.FP32)
     with pytest.raises(ewpt.EwptError, match="2\\^31"):
         ewpt.Ensemble([ewpt.baseline_couplings(N=16, precision=ewpt.FP32), big])
+
+
+def test_ensemble_rejects_bad_tiling():
+    ps = [ewpt.baseline_couplings(N=n, precision=ewpt.FP32) for n in (16, 20)]
+    with ewpt.Ensemble(ps) as ens:
+        # (bx, by, pair): partial warp, more than 128 threads, pair 2
+        for t in [(8, 3, 1), (32, 8, 1), (32, 4, 2)]:
+            with pytest.raises(ewpt.EwptError):
+                ens.set_tiling(*t)
+        ens.set_tiling(16, 8, 1)
+        ens.step(1)
+        ens.sync()

@@ -108,23 +108,29 @@ def log_spectrum(mean: np.ndarray, floor: float = 1e-30) -> np.ndarray:
     return np.log10(np.maximum(mean, 0.0) + floor)
 
 
-def draw_members(n: int, N: int, seed: int):
-    """Seeded uniform draws of (lambda, g, g', bubble count) and the member params."""
+def draw_members(n: int, N, seed: int):
+    """Seeded uniform draws of (lambda, g, g', bubble count) and the member
+    params.  N is one lattice size or a sequence of sizes drawn uniformly per
+    member; with several sizes log2(N) joins the parameter features."""
     rng = np.random.default_rng(seed)
     lam = rng.uniform(0.11, 0.15, n)
     gw = rng.uniform(0.60, 0.70, n)
     gy = rng.uniform(0.32, 0.38, n)
     nb = rng.integers(4, 17, n)
-    ps = [baseline_couplings(N=N, dx=0.25, dt=0.025, lam=float(lam[i]), gw=float(gw[i]), gy=float(gy[i]),
-                             precision=_lib.FP32) for i in range(n)]
-    return ps, np.stack([lam, gw, gy, nb.astype(np.float64)], axis=1), nb
+    sizes = [int(N)] if np.isscalar(N) else [int(v) for v in N]
+    Ns = rng.choice(sizes, n) if len(sizes) > 1 else np.full(n, sizes[0])
+    ps = [baseline_couplings(N=int(Ns[i]), dx=0.25, dt=0.025, lam=float(lam[i]), gw=float(gw[i]),
+                             gy=float(gy[i]), precision=_lib.FP32) for i in range(n)]
+    cols = [lam, gw, gy, nb.astype(np.float64)] + ([np.log2(Ns.astype(np.float64))] if len(sizes) > 1 else [])
+    return ps, np.stack(cols, axis=1), nb
 
 
-def generate_dataset(n_runs: int, N: int = 64, nshell: int = 40, t_early: int = 50, t_late: int = 500,
+def generate_dataset(n_runs: int, N=64, nshell: int = 40, t_early: int = 50, t_late: int = 500,
                      seed: int = 0, chunk: int = 96, verbose: bool = False) -> dict:
     """Evolve n_runs seeded bubble-nucleation runs with the ensemble engine and
     record X = [log B spectrum, log Higgs spectrum at t_early, params] and
-    Y = log B spectrum at t_late (nshell log shells each)."""
+    Y = log B spectrum at t_late (nshell log shells each over [1, N/2] in
+    index units).  N: one size or a sequence of sizes (draw_members)."""
     X, Y, P, E = [], [], [], []
     t0 = time.perf_counter()
     gpu_s = 0.0
@@ -156,7 +162,8 @@ def generate_dataset(n_runs: int, N: int = 64, nshell: int = 40, t_early: int = 
         if verbose:
             print(f"runs {c0 + n}/{n_runs}  {time.perf_counter() - t0:.1f}s", flush=True)
     return dict(X=np.array(X, dtype=np.float32), Y=np.array(Y, dtype=np.float32), params=np.array(P),
-                evolve_seconds=gpu_s, runs=n_runs, N=N, t_early=t_early, t_late=t_late, nshell=nshell)
+                evolve_seconds=gpu_s, runs=n_runs, N=N if np.isscalar(N) else list(N), t_early=t_early,
+                t_late=t_late, nshell=nshell)
 
 
 class Surrogate:
@@ -197,15 +204,18 @@ class Surrogate:
         return self.net.forward(xs) * self.sy + self.my
 
 
-def train_and_evaluate(n_runs: int = 1024, N: int = 48, nshell: int = 40, t_early: int = 50, t_late: int = 500,
+def train_and_evaluate(n_runs: int = 1024, N=48, nshell: int = 40, t_early: int = 50, t_late: int = 500,
                        holdout: float = 0.1, epochs: int = 300, seed: int = 0, verbose: bool = True) -> dict:
     """Generate a dataset with the ensemble engine, train the surrogate on the
     growth of the log B spectrum over persistence, and report held-out errors
-    against the evolved spectra (the judge) and the cost of both paths."""
+    against the evolved spectra (the judge) and the cost of both paths.
+    holdout: a fraction of the runs (< 1) or a number of runs (>= 1)."""
+    t_gen = time.perf_counter()
     data = generate_dataset(n_runs, N=N, nshell=nshell, t_early=t_early, t_late=t_late, seed=seed,
                             verbose=verbose)
+    t_gen = time.perf_counter() - t_gen
     X, Y = data["X"], data["Y"]
-    n_te = max(1, int(round(holdout * n_runs)))
+    n_te = int(holdout) if holdout >= 1 else max(1, int(round(holdout * n_runs)))
     ntr = n_runs - n_te
     early = X[:, :nshell]
     sur = Surrogate(X.shape[1], nshell, width=256, max_batch=512, seed=seed)
@@ -218,7 +228,8 @@ def train_and_evaluate(n_runs: int = 1024, N: int = 48, nshell: int = 40, t_earl
     live = Y[:ntr].std(0) > 1e-3
     Yt = Y[ntr:]
     mse = lambda P: float(np.mean((P - Yt)[:, live] ** 2))
-    report = dict(runs=n_runs, train=ntr, held_out=n_te, N=N, nshell=nshell, t_early=t_early, t_late=t_late,
+    report = dict(runs=n_runs, train=ntr, held_out=n_te, N=data["N"], nshell=nshell, t_early=t_early,
+                  t_late=t_late, dataset_seconds=t_gen,
                   mse_surrogate=mse(pred), mse_mean_baseline=mse(np.broadcast_to(Y[:ntr].mean(0), Yt.shape)),
                   mse_persistence=mse(early[ntr:] + (Y[:ntr] - early[:ntr]).mean(0)),
                   train_seconds=t_train, final_train_loss=hist[-1],
@@ -234,14 +245,17 @@ if __name__ == "__main__":
 
     ap = argparse.ArgumentParser(description="train and evaluate the spectrum surrogate")
     ap.add_argument("--runs", type=int, default=1024)
-    ap.add_argument("--N", type=int, default=48)
+    ap.add_argument("--N", default="48", help="lattice size, or sizes drawn per run: 64,96,128")
+    ap.add_argument("--held-out", type=float, default=0.1, help="fraction (< 1) or number of held-out runs")
     ap.add_argument("--nshell", type=int, default=40)
     ap.add_argument("--t-early", type=int, default=50)
     ap.add_argument("--t-late", type=int, default=500)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--out", default=None, help="write the report JSON here")
     a = ap.parse_args()
-    r = train_and_evaluate(a.runs, a.N, a.nshell, a.t_early, a.t_late, epochs=a.epochs)["report"]
+    sizes = [int(v) for v in a.N.split(",")]
+    r = train_and_evaluate(a.runs, sizes[0] if len(sizes) == 1 else sizes, a.nshell, a.t_early, a.t_late,
+                           holdout=a.held_out, epochs=a.epochs)["report"]
     print(json.dumps(r, indent=1))
     if a.out:
         with open(a.out, "w") as f:

@@ -200,6 +200,26 @@ static int staging64(ewpt_ctx* c, double** out, bool in) {
     return EWPT_OK;
 }
 
+// Copy the 36 arrays between the caller's pointers and a [36][S] buffer,
+// one cudaMemcpyAsync per run of arrays that lie back to back in the
+// caller's memory (a packed state is one copy).
+static cudaError_t copy_runs(double* dev, const double* const* arrays, int64_t S, bool to_dev, int32_t on_device,
+                             cudaStream_t st) {
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice
+                                          : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < 36 && e == cudaSuccess;) {
+        int b = a + 1;
+        while (b < 36 && arrays[b] == arrays[b - 1] + S) ++b;
+        const size_t bytes = (size_t)(b - a) * S * 8;
+        double* d = dev + (size_t)a * S;
+        e = to_dev ? cudaMemcpyAsync(d, arrays[a], bytes, kind, st)
+                   : cudaMemcpyAsync(const_cast<double*>(arrays[a]), d, bytes, kind, st);
+        a = b;
+    }
+    return e;
+}
+
 int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t on_device) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     if (!arrays) return ewpt_fail(c, EWPT_ERR_ARG, "arrays is NULL");
@@ -209,11 +229,7 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
     double* dst;
     int rc = staging64(c, &dst, true);
     if (rc) return rc;
-    const size_t bytes = (size_t)c->g.S * 8;
-    cudaError_t e = cudaSuccess;
-    for (int a = 0; a < 36 && e == cudaSuccess; ++a)
-        e = cudaMemcpyAsync(dst + (size_t)a * c->g.S, arrays[a], bytes,
-                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st);
+    cudaError_t e = copy_runs(dst, arrays, c->g.S, true, on_device, c->st);
     if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, c->lay, dst, c->y32, c->st);
     if (e == cudaSuccess && c->p.precision == EWPT_DF64) e = launch_to_dd(36 * c->g.S, c->y, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -232,10 +248,7 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
     cudaError_t e = cudaSuccess;
     if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->lay, c->y32, src, c->st);
     if (c->p.precision == EWPT_DF64) e = launch_from_dd(36 * c->g.S, c->y, src, c->st);
-    const size_t bytes = (size_t)c->g.S * 8;
-    for (int a = 0; a < 36 && e == cudaSuccess; ++a)
-        e = cudaMemcpyAsync(arrays[a], src + (size_t)a * c->g.S, bytes,
-                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = copy_runs(src, arrays, c->g.S, false, on_device, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     rc = ewpt_cuda_check(c, e, "get_state");
     return rc ? rc : ewpt_tma_check(c);

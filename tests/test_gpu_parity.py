@@ -115,6 +115,33 @@ def test_df64_100_steps_vs_oracle(shape, beta):
     np.testing.assert_allclose(d[:14], do[:14], rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32, ewpt.DF64])
+def test_state_io_separate_and_packed_arrays(prec):
+    """ewpt_set_state / ewpt_get_state with 36 separate host arrays (one copy
+    each; some of them back to back, which the library merges into one
+    copy) give the same state as the packed entry points."""
+    shape = (12, 10, 14)
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, precision=prec)
+    y = perturbed_bubbles(shape, p.dx, 2, seed=4, amp=0.1)
+    L = ewpt._lib
+    # arrays 0-9 back to back in one block, the others separate
+    block = np.ascontiguousarray(y[:10])
+    sep = [np.ascontiguousarray(y[a]) for a in range(10, 36)]
+    ptrs = L.DPA(*([block[a].ctypes.data_as(L.DP) for a in range(10)] + [v.ctypes.data_as(L.DP) for v in sep]))
+    with ewpt.Lattice(p) as lat:
+        lat._chk(lat.L.ewpt_set_state(lat.h, ptrs, 0))
+        packed = lat.get_state()
+        outs = [np.zeros(p.sites) for _ in range(36)]
+        optr = L.DPA(*[o.ctypes.data_as(L.DP) for o in outs])
+        lat._chk(lat.L.ewpt_get_state(lat.h, optr, 0))
+        lat.set_state(y)
+        ref = lat.get_state()
+    np.testing.assert_array_equal(packed, ref)
+    np.testing.assert_array_equal(np.array(outs), ref)
+    if prec == ewpt.FP64:
+        np.testing.assert_array_equal(ref, y)
+
+
 def test_df64_state_roundtrip_and_golden_step(golden_dir):
     """set_state / get_state of a DF64 context is exact to the double-float
     split (2^-48), and one DF64 step matches the golden FP64 step to 1e-12."""

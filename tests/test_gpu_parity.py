@@ -95,6 +95,29 @@ def test_fp64_100_steps_vs_oracle(shape, beta):
     assert rel_err(y, yo) < 1e-11
 
 
+def test_fp64_energy_and_gauss_history_vs_oracle():
+    """The snapshot rows every 10 of 100 steps (13 energy columns, total,
+    the Gauss-constraint norms and maxima) follow the oracle's history."""
+    shape = (24, 20, 28)
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, beta_w=0.2, beta_y=0.1)
+    y0 = perturbed_bubbles(shape, p.dx, 4, seed=21)
+    op = oparams(p)
+    rows, ref = [], []
+    yo = y0.copy()
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        rows.append(lat.diagnostics())
+        ref.append(orc.diagnostics(op, yo))
+        for _ in range(10):
+            lat.step(10, Jex=0.02, gamma=0.01)
+            rows.append(lat.diagnostics())
+            yo = orc.rk4_step(op, yo, p.dt, 0.02, 0.01, nsteps=10)
+            ref.append(orc.diagnostics(op, yo))
+    rows, ref = np.array(rows), np.array(ref)
+    assert np.abs(rows[:, 14:20]).min() > 0  # the constraint is violated: the columns carry signal
+    np.testing.assert_allclose(rows, ref, rtol=1e-10, atol=1e-13)
+
+
 @pytest.mark.parametrize("shape,beta", [((20, 24, 16), True), ((32, 32, 32), False)])
 def test_df64_100_steps_vs_oracle(shape, beta):
     """The DF64 form (FP64 scheme in double-float arithmetic on the FP32

@@ -107,22 +107,14 @@ __global__ void __launch_bounds__(128, 1) k_ens_stage(const EnsMember* __restric
     using T = typename std::conditional<PAIR, f2, float>::type;
     const float* xin = STAGE == 1 ? b.yhi : (STAGE == 3 ? b.xb : b.xa);
     float* xn = STAGE == 1 ? b.xa : (STAGE == 2 ? b.xb : b.xa);
-    // A block's work items increase, so after one binary search its member
-    // only ever advances: one cached bound test per item instead of a
-    // search of dependent loads.
-    int m = blockIdx.x < ntiles ? find_member(tab, nmem, blockIdx.x) : 0;
-    int64_t next0 = m + 1 < nmem ? __ldg(&tab[m + 1].tile0) : ntiles;
     for (int64_t w = blockIdx.x; w < ntiles; w += gridDim.x) {
-        while (w >= next0) {
-            ++m;
-            next0 = m + 1 < nmem ? __ldg(&tab[m + 1].tile0) : ntiles;
-        }
+        const int m = find_member(tab, nmem, w);
         const EnsMember M = tab[m];
-        int t = (int)(w - M.tile0);  // items of one member < 2^31
-        const int tx = t % M.tiles_x;
+        int64_t t = w - M.tile0;
+        const int tx = (int)(t % M.tiles_x);
         t /= M.tiles_x;
-        const int ty = t % M.tiles_y;
-        const int k = t / M.tiles_y;
+        const int ty = (int)(t % M.tiles_y);
+        const int k = (int)(t / M.tiles_y);
         const int i = (tx * (int)blockDim.x + (int)threadIdx.x) * (PAIR ? 2 : 1);
         const int j = ty * (int)blockDim.y + (int)threadIdx.y;
         if (i >= M.nx || j >= M.ny) continue;

@@ -189,7 +189,7 @@ int ewpt_destroy(ewpt_ctx* c) {
 
 // Device buffer holding the packed FP64 state (for FP32 contexts, a staging
 // buffer that split/join convert through).
-static int staging64(ewpt_ctx* c, double** out, bool in) {
+int ewpt_staging64(ewpt_ctx* c, double** out, bool in) {
     if (c->p.precision == EWPT_FP64 || (in && c->p.precision == EWPT_DF64)) {
         *out = c->y;  // DF64: converted in place after the upload
         return EWPT_OK;
@@ -227,13 +227,18 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
     cudaSetDevice(c->p.device);
     double* dst;
-    int rc = staging64(c, &dst, true);
+    int rc = ewpt_staging64(c, &dst, true);
     if (rc) return rc;
     cudaError_t e = copy_runs(dst, arrays, c->g.S, true, on_device, c->st);
-    if (e == cudaSuccess && c->p.precision == EWPT_FP32) e = launch_fp32_split(c->g, c->lay, dst, c->y32, c->st);
-    if (e == cudaSuccess && c->p.precision == EWPT_DF64) e = launch_to_dd(36 * c->g.S, c->y, c->st);
+    if (e == cudaSuccess) e = ewpt_commit_staged(c, dst);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     return ewpt_cuda_check(c, e, "set_state");
+}
+
+cudaError_t ewpt_commit_staged(ewpt_ctx* c, const double* staged) {
+    if (c->p.precision == EWPT_FP32) return launch_fp32_split(c->g, c->lay, staged, c->y32, c->st);
+    if (c->p.precision == EWPT_DF64) return launch_to_dd(36 * c->g.S, c->y, c->st);
+    return cudaSuccess;
 }
 
 int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_device) {
@@ -243,7 +248,7 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
     cudaSetDevice(c->p.device);
     double* src;
-    int rc = staging64(c, &src, false);
+    int rc = ewpt_staging64(c, &src, false);
     if (rc) return rc;
     cudaError_t e = cudaSuccess;
     if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->lay, c->y32, src, c->st);

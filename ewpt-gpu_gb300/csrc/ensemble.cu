@@ -452,6 +452,25 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* e, int32_t m, int32_t nb, const double*
     return EWPT_OK;
 }
 
+int ewpt_ensemble_init_thermal(ewpt_ens* e, int32_t m, double T, double mH, double mW, uint64_t seed) {
+    int rc = ens_member_check(e, m);
+    if (rc) return rc;
+    rc = ewpt_check_thermal(T, mH, mW);
+    if (rc) return ens_fail(e, rc, ewpt_last_error(nullptr));
+    cudaSetDevice(e->device);
+    ewpt_ctx* v;
+    rc = ens_view(e, m, &v);
+    if (rc) return rc;
+    std::string err;
+    rc = ewpt_thermal_fill(v->g, v->p, T, mH, mW, seed, v->y, v->st, &err);  // after the view's join (same stream)
+    if (rc) return ens_fail(e, rc, ("init_thermal: " + err).c_str());
+    const EnsMember& M = e->tab[m];
+    cudaError_t ce =
+        launch_fp32_split(v->g, plain_layout(v->g), v->y, Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, e->st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
+    return ens_cuda(e, ce, "ensemble init_thermal");
+}
+
 int ewpt_ensemble_diagnostics(ewpt_ens* e, int32_t m, double out[EWPT_NDIAG]) {
     int rc = ens_member_check(e, m);
     if (rc) return rc;

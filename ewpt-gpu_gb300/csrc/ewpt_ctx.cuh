@@ -46,6 +46,16 @@ extern "C" int ewpt_create_view(const ewpt_params* p, ewpt_ctx** out);
 // the state joined into c->scratch64.
 int ewpt_state64(ewpt_ctx* c, const double** out);
 int ewpt_ensure_scratch64(ewpt_ctx* c);
+// FP64 [36][S] buffer to write a whole state into (c->y, or the FP32 form's
+// scratch64), and the conversion of a state written there into the
+// context's form (FP32 split with ghost faces, DF64 pairs), on c->st.
+extern "C" int ewpt_staging64(ewpt_ctx* c, double** out, bool in);
+extern "C" cudaError_t ewpt_commit_staged(ewpt_ctx* c, const double* staged);
+// Thermal IC (thermal.cu) into an FP64 [36][S] device state y, synchronous
+// on st; ewpt_check_thermal validates T and the masses.
+int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, double mW, uint64_t seed,
+                      double* y, cudaStream_t st, std::string* err);
+int ewpt_check_thermal(double T, double mH, double mW);
 void ewpt_release_aux(ewpt_ctx* c);
 // Bubble IC kernel (init.cu) on an FP64 state (y) or an FP32 hi/lo state.
 // TMA-staged FP32 stage kernels (stage_tma.cu).

@@ -67,6 +67,7 @@ def _sig(L):
     L.ewpt_rk4_rates.argtypes = [P, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p]
     L.ewpt_diagnostics.argtypes = [V, DP]
     L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
+    L.ewpt_init_thermal.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_uint64]
     L.ewpt_field_components.argtypes = [C.c_int32]
     L.ewpt_field_components.restype = C.c_int32
     L.ewpt_fields.argtypes = [V, C.c_int32, DP, C.c_int32]
@@ -85,6 +86,7 @@ def _sig(L):
     L.ewpt_ensemble_set_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
     L.ewpt_ensemble_get_state.argtypes = [E, C.c_int32, C.c_void_p, C.c_int32]
     L.ewpt_ensemble_set_drive.argtypes = [E, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_ensemble_init_thermal.argtypes = [E, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64]
     L.ewpt_ensemble_set_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_ensemble_step.argtypes = [E, C.c_int32]
     L.ewpt_ensemble_sync.argtypes = [E]

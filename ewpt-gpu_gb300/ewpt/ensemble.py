@@ -4,6 +4,7 @@ graph (ewpt_ensemble_* in include/ewpt.h)."""
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -70,6 +71,15 @@ class Ensemble:
         prof = _lib.BUBBLE_TANH if profile == "tanh" else _lib.BUBBLE_REFERENCE
         self._chk(self.L.ewpt_ensemble_init_bubbles(self.h, m, len(b), b.ctypes.data_as(_lib.DP), prof,
                                                     float(radius), float(width)))
+
+    def init_thermal(self, m: int, T: float, seed: int = 0, mH: float | None = None, mW: float | None = None):
+        """Device thermal IC of member m (ewpt_ensemble_init_thermal); the
+        defaults of Lattice.init_thermal."""
+        p = self.members[m]
+        mH = math.sqrt(2.0 * p.lam) * p.vev if mH is None else mH
+        mW = p.gw * p.vev / 2.0 if mW is None else mW
+        self._chk(self.L.ewpt_ensemble_init_thermal(self.h, m, float(T), float(mH), float(mW),
+                                                    int(seed) & (2 ** 64 - 1)))
 
     def set_drive(self, m: int, Jex: float, gamma: float):
         self._chk(self.L.ewpt_ensemble_set_drive(self.h, m, float(Jex), float(gamma)))

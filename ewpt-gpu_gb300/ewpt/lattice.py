@@ -9,6 +9,7 @@ kernels + host sums (:6451-6805) become `diagnostics()`, and fft + convolve_1d
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -110,6 +111,15 @@ class Lattice:
         prof = _lib.BUBBLE_TANH if profile == "tanh" else _lib.BUBBLE_REFERENCE
         self._chk(self.L.ewpt_init_bubbles(self.h, len(b), b.ctypes.data_as(_lib.DP), prof, float(radius),
                                            float(width)))
+
+    def init_thermal(self, T: float, seed: int = 0, mH: float | None = None, mW: float | None = None):
+        """Device thermal IC (ewpt_init_thermal): Bose-Einstein modes at T,
+        Higgs mass mH (default sqrt(2 lambda) vev), W mass mW (default
+        g vev / 2), Gamma/Sigma = divergence of W/Y, momenta zero."""
+        p = self.params
+        mH = math.sqrt(2.0 * p.lam) * p.vev if mH is None else mH
+        mW = p.gw * p.vev / 2.0 if mW is None else mW
+        self._chk(self.L.ewpt_init_thermal(self.h, float(T), float(mH), float(mW), int(seed) & (2 ** 64 - 1)))
 
     # ------------------------------------------------------------ observables
     def diagnostics(self, allow_nonfinite: bool = False) -> np.ndarray:

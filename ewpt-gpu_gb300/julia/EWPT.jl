@@ -93,6 +93,14 @@ function spectrum(L::Lattice; field=0, mode=0, nbins=40)
     (k=k[1:n[]], sum=s[1:n[]], count=c[1:n[]], mean=m[1:n[]])
 end
 
+"""Thermal initial condition on the device (ewpt_init_thermal): Bose-Einstein
+modes at temperature T with Higgs mass mH and W mass mW (defaults sqrt(2 lambda) vev
+and g vev / 2), Gamma/Sigma the divergence of W/Y, momenta zero; `seed` fixes the state."""
+function init_thermal!(L::Lattice, T; seed::Integer=0, mH=sqrt(2 * L.p.lambda) * L.p.vev, mW=L.p.gw * L.p.vev / 2)
+    check(ccall((:ewpt_init_thermal, libewpt), Cint, (Ptr{Cvoid}, Float64, Float64, Float64, UInt64),
+                L.h, T, mH, mW, UInt64(seed)), L.h)
+end
+
 """Per-site fields as Julia arrays (nx, ny, nz, ncomp): field 0 = B_x,B_y,B_z
 (the E_t of compute_Bx/By/Bz!), 1 = B_2, 2 = phi_1..phi_4, 3 = the energy
 densities PE, KE, GE, EEW, MEW, EEY, MEY (compute_PE! .. compute_MEY!).

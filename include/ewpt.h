@@ -200,6 +200,17 @@ enum ewpt_bubble_profile { EWPT_BUBBLE_REFERENCE = 0, EWPT_BUBBLE_TANH = 1 };
  *   units, r the minimum-image distance (p0 = radius, p1 = wall width). */
 int ewpt_init_bubbles(ewpt_ctx* ctx, int32_t nb, const double* bubbles, int32_t profile, double p0, double p1);
 
+/* Thermal initial condition generated on the device (replaces the thermal
+ * branch of run(), main_rk4.jl:5348-5636, with thermal_initializer_phi! and
+ * thermal_initializer_gauge!, :5029-5152): Bose-Einstein modes at
+ * temperature T as real(bfft(amp (a + i b))), amp = sqrt(n(w) / (w V)),
+ * a, b ~ N(0, sqrt 2); Higgs w^2 = k^2 + mH^2; W^a and Y with two transverse
+ * polarisations and w^2 = k^2 + mW^2 (W) or k^2 (Y); Gamma^a and Sigma set
+ * to the stencil divergence of W^a and Y; momenta zero.  Deviates are a
+ * counter-based hash of (seed, field, mode): the state depends only on the
+ * seed and the lattice.  Resets the iteration counter.  Synchronous. */
+int ewpt_init_thermal(ewpt_ctx* ctx, double T, double mH, double mW, uint64_t seed);
+
 /* ---------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which runs one
  * realization per process; each member here is an independent lattice with
@@ -222,6 +233,9 @@ int ewpt_ensemble_get_state(ewpt_ens* ens, int32_t m, double* packed, int32_t on
 /* ewpt_init_bubbles for member m */
 int ewpt_ensemble_init_bubbles(ewpt_ens* ens, int32_t m, int32_t nb, const double* bubbles, int32_t profile,
                                double p0, double p1);
+/* ewpt_init_thermal for member m (the same state as a single context of
+ * the member's parameters and the same seed, split into the FP32 form) */
+int ewpt_ensemble_init_thermal(ewpt_ens* ens, int32_t m, double T, double mH, double mW, uint64_t seed);
 /* constant Jex and gamma of member m for the following steps */
 int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
 /* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent

@@ -11,8 +11,11 @@ shape) and the DF64 form, from identical inputs.  The FP64 form is the
 reference here: it matches the CPU oracle to 1e-11 per field over 100 steps
 (tests), and the oracle itself cannot evolve these lattices in useful time.
 
-`--gauss-iters` sets the fixed-point iterations of the Gauss projection of
-the initial electric fields (each one removes about half of the remaining
+`--device-ic` starts every form from the device thermal IC instead
+(ewpt_init_thermal with the seed: the reference's construction, momenta
+zero, generated in milliseconds at any size).  `--gauss-iters` sets the
+fixed-point iterations of the host IC's Gauss projection of the initial
+electric fields (each one removes about half of the remaining
 constraint residual; 20 leave ~1e-7 of the charge density).  `--forms`
 picks the forms; fp64 always runs, as the reference.
 
@@ -37,9 +40,14 @@ from .params import baseline_couplings
 
 
 def evolve(p, y0, steps, every, tune=True):
+    """y0: the (36, S) initial state, or ("device", T, seed) for the device
+    thermal IC (identical in every form up to the form's storage)."""
     hist, t0 = [], time.perf_counter()
     with Lattice(p) as lat:
-        lat.set_state(y0)
+        if isinstance(y0, tuple):
+            lat.init_thermal(y0[1], seed=y0[2])
+        else:
+            lat.set_state(y0)
         tile = autotune.tune(lat) if tune else None
         d = lat.diagnostics(allow_nonfinite=True)
         hist.append([0, d[13], d[14], d[16]])
@@ -64,10 +72,11 @@ def rel_field_err(a, b):
 FORMS = {"fp64": _lib.FP64, "fp32": _lib.FP32, "df64": _lib.DF64}
 
 
-def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df64"), gauss_iters=20):
+def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df64"), gauss_iters=20,
+           device_ic=False):
     shape = (N, N, N)
     t0 = time.perf_counter()
-    y0 = ic.thermal(shape, 0.25, T=T, seed=seed, gauss_iters=gauss_iters)
+    y0 = ("device", T, seed) if device_ic else ic.thermal(shape, 0.25, T=T, seed=seed, gauss_iters=gauss_iters)
     t_ic = time.perf_counter() - t0
     runs = {}
     for name in ["fp64"] + [f for f in forms if f != "fp64"]:
@@ -80,7 +89,8 @@ def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df
     E0 = ref["hist"][0, 1]
     smask = ref["spec"] > 1e-12 * ref["spec"].max()
     out = dict(lattice=list(shape), steps=steps, every=every, T=T, seed=seed, dt=0.025, dx=0.25,
-               gauss_iters=gauss_iters, ic_seconds=t_ic, forms={})
+               ic="device (momenta zero)" if device_ic else f"host (Gauss projection, {gauss_iters} iterations)",
+               ic_seconds=t_ic, forms={})
     for name, r in runs.items():
         h = r["hist"]
         f = dict(seconds=r["seconds"], tile=r["tile"],
@@ -106,13 +116,15 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--forms", default="fp64,fp32,df64")
     ap.add_argument("--gauss-iters", type=int, default=20)
+    ap.add_argument("--device-ic", action="store_true",
+                    help="the device thermal IC (ewpt_init_thermal: the reference's construction, momenta zero)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     forms = [f for f in a.forms.split(",") if f]
     bad = [f for f in forms if f not in FORMS]
     if bad:
         ap.error(f"unknown forms {bad}; choose from {sorted(FORMS)}")
-    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters)
+    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters, a.device_ic)
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:

@@ -6,7 +6,7 @@ and backward kernels and AdamW) maps the early-time spectra of a run (B and
 Higgs, `nshell` log shells each) plus its parameters (lambda, g, g', bubble
 count) to the late-time log B spectrum.  Training data come from the
 library's batched ensemble engine (seeded uniform parameter draws, device
-bubble ICs); the plain evolution is the fallback and the judge of the
+bubble or thermal ICs); the plain evolution is the fallback and the judge of the
 surrogate's error, and the surrogate never replaces the evolution path.
 """
 from __future__ import annotations
@@ -108,10 +108,13 @@ def log_spectrum(mean: np.ndarray, floor: float = 1e-30) -> np.ndarray:
     return np.log10(np.maximum(mean, 0.0) + floor)
 
 
-def draw_members(n: int, N, seed: int):
+def draw_members(n: int, N, seed: int, thermal_fraction: float = 0.0):
     """Seeded uniform draws of (lambda, g, g', bubble count) and the member
     params.  N is one lattice size or a sequence of sizes drawn uniformly per
-    member; with several sizes log2(N) joins the parameter features."""
+    member; with several sizes log2(N) joins the parameter features.  With
+    thermal_fraction > 0 that share of the runs starts from the thermal IC
+    at T in [1, 2] vev instead of bubbles (bubble count 0), and T joins the
+    features (0 for bubble runs)."""
     rng = np.random.default_rng(seed)
     lam = rng.uniform(0.11, 0.15, n)
     gw = rng.uniform(0.60, 0.70, n)
@@ -121,12 +124,19 @@ def draw_members(n: int, N, seed: int):
     Ns = rng.choice(sizes, n) if len(sizes) > 1 else np.full(n, sizes[0])
     ps = [baseline_couplings(N=int(Ns[i]), dx=0.25, dt=0.025, lam=float(lam[i]), gw=float(gw[i]),
                              gy=float(gy[i]), precision=_lib.FP32) for i in range(n)]
-    cols = [lam, gw, gy, nb.astype(np.float64)] + ([np.log2(Ns.astype(np.float64))] if len(sizes) > 1 else [])
+    cols = [lam, gw, gy]
+    if thermal_fraction > 0:
+        Ts = np.where(rng.random(n) < thermal_fraction, rng.uniform(1.0, 2.0, n), 0.0)
+        nb = np.where(Ts > 0, 0, nb)
+        cols += [nb.astype(np.float64), Ts]
+    else:
+        cols += [nb.astype(np.float64)]
+    cols += [np.log2(Ns.astype(np.float64))] if len(sizes) > 1 else []
     return ps, np.stack(cols, axis=1), nb
 
 
 def generate_dataset(n_runs: int, N=64, nshell: int = 40, t_early: int = 50, t_late: int = 500,
-                     seed: int = 0, chunk: int = 96, verbose: bool = False) -> dict:
+                     seed: int = 0, chunk: int = 96, verbose: bool = False, thermal_fraction: float = 0.0) -> dict:
     """Evolve n_runs seeded bubble-nucleation runs with the ensemble engine and
     record X = [log B spectrum, log Higgs spectrum at t_early, params] and
     Y = log B spectrum at t_late (nshell log shells each over [1, N/2] in
@@ -136,12 +146,15 @@ def generate_dataset(n_runs: int, N=64, nshell: int = 40, t_early: int = 50, t_l
     gpu_s = 0.0
     for c0 in range(0, n_runs, chunk):
         n = min(chunk, n_runs - c0)
-        ps, prm, nb = draw_members(n, N, seed * 100003 + c0)
+        ps, prm, nb = draw_members(n, N, seed * 100003 + c0, thermal_fraction)
         with Ensemble(ps) as ens:
             for m, p in enumerate(ps):
-                R, w = ic.tanh_profile_params(p.lam, p.vev)
-                bl = ic.tanh_bubble_list(p.dims, p.dx, int(nb[m]), seed=seed * 7919 + c0 + m)
-                ens.init_bubbles(m, bl, "tanh", R, w)
+                if nb[m] > 0:
+                    R, w = ic.tanh_profile_params(p.lam, p.vev)
+                    bl = ic.tanh_bubble_list(p.dims, p.dx, int(nb[m]), seed=seed * 7919 + c0 + m)
+                    ens.init_bubbles(m, bl, "tanh", R, w)
+                else:  # thermal run: T is the feature after the bubble count
+                    ens.init_thermal(m, float(prm[m, 4]) * p.vev, seed=seed * 7919 + c0 + m)
             ts = time.perf_counter()
             ens.step(t_early)
             ens.sync()
@@ -205,14 +218,15 @@ class Surrogate:
 
 
 def train_and_evaluate(n_runs: int = 1024, N=48, nshell: int = 40, t_early: int = 50, t_late: int = 500,
-                       holdout: float = 0.1, epochs: int = 300, seed: int = 0, verbose: bool = True) -> dict:
+                       holdout: float = 0.1, epochs: int = 300, seed: int = 0, verbose: bool = True,
+                       thermal_fraction: float = 0.0) -> dict:
     """Generate a dataset with the ensemble engine, train the surrogate on the
     growth of the log B spectrum over persistence, and report held-out errors
     against the evolved spectra (the judge) and the cost of both paths.
     holdout: a fraction of the runs (< 1) or a number of runs (>= 1)."""
     t_gen = time.perf_counter()
     data = generate_dataset(n_runs, N=N, nshell=nshell, t_early=t_early, t_late=t_late, seed=seed,
-                            verbose=verbose)
+                            verbose=verbose, thermal_fraction=thermal_fraction)
     t_gen = time.perf_counter() - t_gen
     X, Y = data["X"], data["Y"]
     n_te = int(holdout) if holdout >= 1 else max(1, int(round(holdout * n_runs)))
@@ -229,7 +243,7 @@ def train_and_evaluate(n_runs: int = 1024, N=48, nshell: int = 40, t_early: int 
     Yt = Y[ntr:]
     mse = lambda P: float(np.mean((P - Yt)[:, live] ** 2))
     report = dict(runs=n_runs, train=ntr, held_out=n_te, N=data["N"], nshell=nshell, t_early=t_early,
-                  t_late=t_late, dataset_seconds=t_gen,
+                  t_late=t_late, thermal_fraction=thermal_fraction, dataset_seconds=t_gen,
                   mse_surrogate=mse(pred), mse_mean_baseline=mse(np.broadcast_to(Y[:ntr].mean(0), Yt.shape)),
                   mse_persistence=mse(early[ntr:] + (Y[:ntr] - early[:ntr]).mean(0)),
                   train_seconds=t_train, final_train_loss=hist[-1],
@@ -247,6 +261,7 @@ if __name__ == "__main__":
     ap.add_argument("--runs", type=int, default=1024)
     ap.add_argument("--N", default="48", help="lattice size, or sizes drawn per run: 64,96,128")
     ap.add_argument("--held-out", type=float, default=0.1, help="fraction (< 1) or number of held-out runs")
+    ap.add_argument("--thermal-fraction", type=float, default=0.0, help="share of thermal-IC runs (T in [1, 2])")
     ap.add_argument("--nshell", type=int, default=40)
     ap.add_argument("--t-early", type=int, default=50)
     ap.add_argument("--t-late", type=int, default=500)
@@ -255,7 +270,7 @@ if __name__ == "__main__":
     a = ap.parse_args()
     sizes = [int(v) for v in a.N.split(",")]
     r = train_and_evaluate(a.runs, sizes[0] if len(sizes) == 1 else sizes, a.nshell, a.t_early, a.t_late,
-                           holdout=a.held_out, epochs=a.epochs)["report"]
+                           holdout=a.held_out, epochs=a.epochs, thermal_fraction=a.thermal_fraction)["report"]
     print(json.dumps(r, indent=1))
     if a.out:
         with open(a.out, "w") as f:

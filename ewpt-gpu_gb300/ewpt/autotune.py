@@ -109,7 +109,9 @@ def best_tiling(p: Params, steps: int = 2, use_cache: bool = True) -> tuple:
 
 
 def tune(lat: Lattice, steps: int = 2) -> tuple:
-    """Apply the cached (or freshly measured) best tiling to `lat`."""
+    """Apply the cached (or freshly measured) best tiling to `lat`.  A sweep
+    runs on a second lattice of the same size: for lattices that fill most
+    of the GPU, call best_tiling(params) before creating the lattice."""
     tile = best_tiling(lat.params, steps)
     lat.set_tiling(*tile)
     return tile

@@ -43,12 +43,15 @@ def evolve(p, y0, steps, every, tune=True):
     """y0: the (36, S) initial state, or ("device", T, seed) for the device
     thermal IC (identical in every form up to the form's storage)."""
     hist, t0 = [], time.perf_counter()
+    # the sweep runs on its own scratch lattice: pick the shape before this one exists
+    tile = autotune.best_tiling(p) if tune else None
     with Lattice(p) as lat:
         if isinstance(y0, tuple):
             lat.init_thermal(y0[1], seed=y0[2])
         else:
             lat.set_state(y0)
-        tile = autotune.tune(lat) if tune else None
+        if tile:
+            lat.set_tiling(*tile)
         d = lat.diagnostics(allow_nonfinite=True)
         hist.append([0, d[13], d[14], d[16]])
         done = 0

@@ -178,7 +178,7 @@ def _div(fx, fy, fz, sym):
 
 def thermal(shape, dx, T=1.5, lam=0.129, gw=0.65, gy=0.35, vev=1.0, seed=0, mH=None, mW=None,
             gauss_iters=20, with_momenta=True):
-    """Thermal initial condition (BASELINE precision configuration).
+    """Thermal initial condition of the precision configuration (thermal IC, T = 1.5 vev).
 
     Gaussian random Higgs and gauge modes with Bose-Einstein occupation
     n(w) = 1/(exp(w/T) - 1): Higgs w^2 = k^2 + mH^2 (mH = sqrt(2 lambda) vev),

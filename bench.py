@@ -42,11 +42,12 @@ METRIC = "site-updates/s per RK4 step at 256³ (FP64 vs FP32 form), % of HBM pea
 BYTES_FP64 = 3744  # 468 FP64 values per site-update (k-storage RK4)
 BYTES_FP32 = 2592  # y in FP64 width, stage rates in FP32
 # DRAM bytes per site-update (sum over the 4 stage launches) from one ncu
-# capture of the stage kernels at 80^3 (dram__bytes_read.sum +
-# dram__bytes_write.sum); traffic grows with the site count, so a 256^3
-# launch moves this x S / 4.
+# capture of the stage kernels (dram__bytes_read.sum + dram__bytes_write.sum):
+# FP64 at 80^3, 32x2 threads; FP32 form at 128^3, the tuned paired kernel
+# (64x2 pair-threads, <= 168 registers).  Traffic grows with the site count,
+# so a 256^3 launch moves this x S / 4.
 TRAFFIC_FP64 = 4383
-TRAFFIC_FP32 = 2686
+TRAFFIC_FP32 = 2804
 N_BUBBLES = 64
 
 
@@ -292,6 +293,7 @@ def run_ours(args, ws, rank, local):
                             "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm, "unit": "GB/s",
                                          "frac": a32 / hbm, "peak_kind": peak_kind,
                                          "traffic": TRAFFIC_FP32 * S / 4,
+                                         "traffic_source": "ncu dram bytes per site-update at 128^3 x sites / 4",
                                          "launch_ms": f["t"] / f["steps"] / 4 * 1e3,
                                          "algorithmic_bytes_per_site_update": BYTES_FP32}}
     if "df64" in res:

@@ -337,9 +337,7 @@ int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pa
         c->tile = Tiling{bx, by, reg, pair};
         return EWPT_OK;
     }
-    if (reg < 0 || reg > 3) return ewpt_fail(c, EWPT_ERR_ARG, "register variant %d unknown (0..3)", reg);
-    if (reg == 3 && c->p.precision != EWPT_DF64)
-        return ewpt_fail(c, EWPT_ERR_ARG, "register variant 3 (phase-synchronised blocks) is the DF64 form's");
+    if (reg < 0 || reg > 2) return ewpt_fail(c, EWPT_ERR_ARG, "register variant %d unknown (0..2)", reg);
     if (bx < 1 || by < 1 || bx * by > tiling_max_threads(reg) || (bx * by) % 32 != 0)
         return ewpt_fail(c, EWPT_ERR_ARG, "tile %dx%d: need whole warps and at most %d threads for variant %d", bx, by,
                          tiling_max_threads(reg), reg);

@@ -30,25 +30,7 @@
 //   grad_lap(a, gx, gy, gz, lap)   first derivatives and Laplacian
 //   div3(a)                        dx(a) + dy(a+1) + dz(a+2)
 // Sink `out(a, rate)` receives rate a = d y_a / dt exactly once.
-//
-// Phase points: an accessor type with `static constexpr bool kPhaseSync =
-// true` makes the block synchronise (__syncthreads) at the boundaries of
-// the blocks of work below.  The kernel using it must keep every thread of
-// the block on this path (no early exit).  It exists for instruction-fetch-
-// bound forms whose straight-line code exceeds the instruction cache: warps
-// that stay in one phase share the fetched instructions.
 #pragma once
-#include <type_traits>
-
-template <class A, class = void>
-struct phase_sync : std::false_type {};
-template <class A>
-struct phase_sync<A, std::void_t<decltype(A::kPhaseSync)>> : std::bool_constant<A::kPhaseSync> {};
-
-template <class Acc>
-__device__ __forceinline__ void phase_point(const Acc&) {
-    if constexpr (phase_sync<Acc>::value) __syncthreads();
-}
 
 template <typename T>
 struct PhysCoef {
@@ -87,7 +69,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     // ---- k_field = momentum (main_rk4.jl:585-600)
 #pragma unroll
     for (int a = 0; a < 16; ++a) out(a, A.v(20 + a));
-    phase_point(A);
 
     // ---- k_Gamma_a, k_Sigma (main_rk4.jl:603-655)
     {
@@ -111,7 +92,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         }
         out(19, c.omgp2 * A.div3(33) + c.gp2 * gy * (p1 * pt2 - p2 * pt1 + p3 * pt4 - p4 * pt3));
     }
-    phase_point(A);
 
     // ---- Higgs block: gradients, covariant derivatives, kt_phi (main_rk4.jl:337-407)
     T ktp1, ktp2, ktp3, ktp4;
@@ -121,10 +101,8 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         T d1[3], d2[3], d3[3], d4[3], l1, l2, l3, l4;
         A.grad_lap(0, d1[0], d1[1], d1[2], l1);
         A.grad_lap(1, d2[0], d2[1], d2[2], l2);
-        phase_point(A);
         A.grad_lap(2, d3[0], d3[1], d3[2], l3);
         A.grad_lap(3, d4[0], d4[1], d4[2], l4);
-        phase_point(A);
         const T Yv[3] = {Y2, Y3, Y4};
         T D1[3], D2[3], D3[3], D4[3];
 #pragma unroll
@@ -151,7 +129,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
                c.hJex * p4 - c.gam * p4 * (p4 * pt4) * inv_mag;
 #undef WD
 #undef YD
-        phase_point(A);
         // Higgs currents of kt_W (main_rk4.jl:415,432,449,...) and kt_Y (:563)
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -179,7 +156,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     }
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-        phase_point(A);
         T dW[3][3];  // dW[i][j] = d_j W^b_i
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -198,7 +174,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
             ktW[b1][i] += gw * (dW[i][0] * W[b2][0] + dW[i][1] * W[b2][1] + dW[i][2] * W[b2][2]);
         }
     }
-    phase_point(A);
     // -g sum_j (W^b_j F^c_ij - W^c_j F^b_ij) with F_ij antisymmetric
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -211,7 +186,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         ktW[a][2] -= gw * ((W[cc][0] * F[b][1] - W[b][0] * F[cc][1]) + (W[cc][1] * F[b][2] - W[b][1] * F[cc][2]));
     }
     // auxiliary gradient
-    phase_point(A);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         T gx, gy_, gz;
@@ -222,7 +196,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     }
 
     // ---- U(1) block (field_strengths.jl:281-311, main_rk4.jl:562-581)
-    phase_point(A);
     T ktY[3], FY[3];
     {
         T dY[3][3], lap[3];
@@ -239,7 +212,6 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     }
 
     // ---- beta (CP-odd) terms
-    phase_point(A);
     if (BETA) {
         T Wt[3][3];
 #pragma unroll

@@ -247,7 +247,7 @@ Ptr36 pack(const void* base, int64_t S, size_t elem) {
 
 }  // namespace
 
-int tiling_max_threads(int reg) { return reg >= 0 && reg <= 2 ? 128 : reg == 3 ? 384 : 0; }
+int tiling_max_threads(int reg) { return reg >= 0 && reg <= 2 ? 128 : 0; }
 
 cudaError_t launch_rates_fp64(const Grid& g, const Ptr36& in, const MPtr36& out, const ewpt_params& p,
                               double Jex, double gam, cudaStream_t st) {

@@ -12,31 +12,18 @@
 
 namespace {
 
-// Register budgets: 0 = the compiler's choice, 2 = at most 168 registers
-// (3 blocks of 128 threads per SM), 3 = at most 168 registers in one block
-// of 384 threads per SM whose warps synchronise at the phase points of
-// site_rates.  The DF64 stage is ~20 k instructions of straight-line code per
-// thread; with warps spread over all of it, instruction fetch stalls
-// dominate (ncu: no_instruction ~6 cycles per issued instruction).  Keeping
-// the 12 warps of an SM inside one phase lets them share the fetched code.
 template <int REG>
 struct DdBudget;
 template <>
 struct DdBudget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <>
 struct DdBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
-template <>
-struct DdBudget<3> { static constexpr int kThreads = 384, kMinBlocks = 1; };
 
 using DdAcc = SiteAcc<float2, dd, SrcPtr36<float2>>;
-struct DdAccPhased : DdAcc {
-    static constexpr bool kPhaseSync = true;
-};
 
 template <int STAGE>
 struct DdSink {
     const DdAcc& A;
-    bool active;  // false for the clamped stand-in sites of partial blocks
     const float2* __restrict__ y;
     float2* yn;
     float2* __restrict__ xn;
@@ -44,7 +31,6 @@ struct DdSink {
     int64_t S;
     dd w, h;
     __device__ __forceinline__ void operator()(int a, dd r) const {
-        if (!active) return;
         const int64_t q = a * S + A.c;
         if (STAGE == 1) {
             const dd ya = A.v(a);  // X1 == y
@@ -67,23 +53,12 @@ __global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBl
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    const bool active = i < g.nx && j < g.ny;
-    if constexpr (REG == 3) {
-        // every thread runs to the end (the phase points are block barriers):
-        // threads past the edge evaluate a clamped site and store nothing
-        DdAccPhased A{{{X}}};
-        A.place(min(i, g.nx - 1), min(j, g.ny - 1), k, g.nx, g.ny, g.nz);
-        A.s = sc;
-        DdSink<STAGE> out{A, active, y, yn, xn, acc_out, g.S, w, h};
-        site_rates<dd, BETA>(A, pc, out);
-    } else {
-        if (!active) return;
-        DdAcc A{{X}};
-        A.place(i, j, k, g.nx, g.ny, g.nz);
-        A.s = sc;
-        DdSink<STAGE> out{A, true, y, yn, xn, acc_out, g.S, w, h};
-        site_rates<dd, BETA>(A, pc, out);
-    }
+    if (i >= g.nx || j >= g.ny) return;
+    DdAcc A{{X}};
+    A.place(i, j, k, g.nx, g.ny, g.nz);
+    A.s = sc;
+    DdSink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};
+    site_rates<dd, BETA>(A, pc, out);
 }
 
 __global__ void k_to_dd(int64_t n, double* __restrict__ v) {
@@ -119,9 +94,7 @@ template <bool BETA>
 void step_dd_r(const Grid& g, const Tiling& t, float2* y, float2* yn, float2* xa, float2* xb, const PhysCoef<dd>& pc,
                const StencilCoef<dd>& sc, double dt, cudaStream_t st) {
     // the 128-register variant spills heavily in this form and runs as variant 0
-    if (t.reg == 3)
-        step_dd<BETA, 3>(g, t, y, yn, xa, xb, pc, sc, dt, st);
-    else if (t.reg == 2)
+    if (t.reg == 2)
         step_dd<BETA, 2>(g, t, y, yn, xa, xb, pc, sc, dt, st);
     else
         step_dd<BETA, 0>(g, t, y, yn, xa, xb, pc, sc, dt, st);

@@ -24,8 +24,6 @@ PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (
                    (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1)]
 # FP32 form only: TMA-staged tiles of 32 x by x bz sites, (bx, by, bz, 2)
 TMA_CANDIDATES = [(32, 4, 4, 2), (32, 2, 4, 2)]
-# DF64 form only: one 384-thread block per SM, warps synchronised per phase
-PHASED_CANDIDATES = [(64, 6, 3, 0), (32, 12, 3, 0), (128, 3, 3, 0), (64, 4, 3, 0)]
 
 
 def cache_path() -> str:
@@ -85,8 +83,6 @@ def sweep(p: Params, steps: int = 2, candidates=None) -> list:
         nx, ny, nz = p.dims
         if int(p.precision) == _lib.FP32 and nx % 32 == 0:
             candidates += [t for t in TMA_CANDIDATES if ny % t[1] == 0 and nz % t[2] == 0]
-        if int(p.precision) == _lib.DF64:
-            candidates += PHASED_CANDIDATES
     res = []
     with Lattice(p) as lat:
         R, w = ic.tanh_profile_params(p.lam, p.vev)

@@ -110,10 +110,7 @@ int64_t ewpt_iteration(const ewpt_ctx* ctx);
 /* Launch shape of the stage kernels.  pair = 0 or 1: blocks of bx*by
  * threads over x and y (whole warps, at most 128 threads), reg = register-
  * budget variant (0: registers at the compiler's choice; 1: <= 128
- * registers; 2: <= 168; 3, DF64 form only: <= 168 in blocks of up to 384
- * threads whose warps synchronise between the phases of the stage, so that
- * they share the instruction fetch of its long straight-line code); pair = 1
- * (FP32 form, even nx): each thread evolves
+ * registers; 2: <= 168); pair = 1 (FP32 form, even nx): each thread evolves
  * two x-adjacent sites with packed FP32x2 arithmetic.  pair = 2 (FP32 form):
  * TMA-staged shared-memory tiles of bx x by x reg sites -- bx = 32, by = 4 or
  * 2, reg = 4 (the tile's z extent); needs nx % 32 == 0, ny % by == 0,

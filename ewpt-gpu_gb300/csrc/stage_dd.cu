@@ -19,7 +19,17 @@ struct DdBudget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <>
 struct DdBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
 
-using DdAcc = SiteAcc<float2, dd, SrcPtr36<float2>>;
+// The stencil evaluations are out-of-line calls: the double-float stage is
+// instruction-fetch bound (~20 k straight-line instructions per site), and
+// one copy of each stencil routine replaces 16 + 4 + 4 inlined copies.
+struct DdAcc : SiteAcc<float2, dd, SrcPtr36<float2>> {
+    using Base = SiteAcc<float2, dd, SrcPtr36<float2>>;
+    __device__ __noinline__ void grad_lap(int a, dd& gx, dd& gy, dd& gz, dd& lap) const {
+        Base::grad_lap(a, gx, gy, gz, lap);
+    }
+    __device__ __noinline__ void grad(int a, dd& gx, dd& gy, dd& gz) const { Base::grad(a, gx, gy, gz); }
+    __device__ __noinline__ dd div3(int a) const { return Base::div3(a); }
+};
 
 template <int STAGE>
 struct DdSink {
@@ -54,7 +64,7 @@ __global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBl
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return;
-    DdAcc A{{X}};
+    DdAcc A{{{X}}};
     A.place(i, j, k, g.nx, g.ny, g.nz);
     A.s = sc;
     DdSink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};

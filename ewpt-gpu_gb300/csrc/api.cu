@@ -122,6 +122,7 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         if (e == cudaSuccess) e = cudaMalloc(&c->yn, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->xa, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->xb, n * 8);
+        if (e == cudaSuccess && p->precision == EWPT_DF64) e = cudaMalloc(&c->ddcur, (size_t)9 * c->g.S * 8);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->y, 0, n * 8, c->st);
     } else {
         // ghosted layout; zero everything so the ghost cells no kernel writes
@@ -175,6 +176,7 @@ int ewpt_destroy(ewpt_ctx* c) {
     cudaFree(c->yn);
     cudaFree(c->xa);
     cudaFree(c->xb);
+    cudaFree(c->ddcur);
     ewpt_tma_release(c);
     cudaFree(c->y32.hi);
     cudaFree(c->y32.lo);
@@ -300,7 +302,7 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
         else if (c->p.precision == EWPT_FP64)
             e = launch_step_fp64(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
         else if (c->p.precision == EWPT_DF64)
-            e = launch_step_dd(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+            e = launch_step_dd(c->g, c->tile, c->y, c->yn, c->xa, c->xb, c->ddcur, c->p, J, G, c->st);
         else if (c->tile.pair == 2)
             e = launch_step_fp32_tma(c, J, G);
         else

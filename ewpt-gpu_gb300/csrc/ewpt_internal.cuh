@@ -158,7 +158,7 @@ cudaError_t launch_rates_fp64_order(const Grid& g, const Ptr36& in, const MPtr36
                                     double Jex, double gam, cudaStream_t st);
 // DF64 form (stage_dd.cu): y, yn, xa, xb hold float pairs (hi, lo).
 cudaError_t launch_step_dd(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
-                           const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+                           double* cur, const ewpt_params& p, double Jex, double gam, cudaStream_t st);
 cudaError_t launch_to_dd(int64_t n, double* v, cudaStream_t st);  // in place: double -> (hi, lo)
 cudaError_t launch_from_dd(int64_t n, const double* src, double* dst, cudaStream_t st);
 cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,

@@ -40,6 +40,9 @@ struct DdSink {
     float2* acc_out;
     int64_t S;
     dd w, h;
+    float2* cur;  // [9][S] Higgs current of kt W, from the first to the second launch of a split stage
+    __device__ __forceinline__ void keep_current(int q, dd v) const { cur[q * S + A.c] = v.f2(); }
+    __device__ __forceinline__ dd load_current(int q) const { return dd(__ldg(cur + q * S + A.c)); }
     __device__ __forceinline__ void operator()(int a, dd r) const {
         const int64_t q = a * S + A.c;
         if (STAGE == 1) {
@@ -56,10 +59,20 @@ struct DdSink {
     }
 };
 
-template <int STAGE, bool BETA, int REG>
+Ptr36 pack8(const void* base, int64_t S) {
+    Ptr36 P;
+    for (int a = 0; a < 36; ++a) P.p[a] = static_cast<const char*>(base) + (size_t)a * S * 8;
+    return P;
+}
+
+// PART (site_rates): 0 the whole stage; 1 and 2 its two halves, launched one
+// after the other when there are no beta terms -- each half is about half
+// of the straight-line code, which is what limits this form.
+template <int STAGE, bool BETA, int REG, int PART>
 __global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBlocks)
     k_stage_dd(Grid g, const __grid_constant__ Ptr36 X, const float2* __restrict__ y, float2* yn,
-               float2* __restrict__ xn, float2* acc_out, PhysCoef<dd> pc, StencilCoef<dd> sc, dd w, dd h) {
+               float2* __restrict__ xn, float2* acc_out, PhysCoef<dd> pc, StencilCoef<dd> sc, dd w, dd h,
+               float2* cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -67,8 +80,8 @@ __global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBl
     DdAcc A{{{X}}};
     A.place(i, j, k, g.nx, g.ny, g.nz);
     A.s = sc;
-    DdSink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h};
-    site_rates<dd, BETA>(A, pc, out);
+    DdSink<STAGE> out{A, y, yn, xn, acc_out, g.S, w, h, cur};
+    site_rates<dd, BETA, DdAcc, DdSink<STAGE>, PART>(A, pc, out);
 }
 
 __global__ void k_to_dd(int64_t n, double* __restrict__ v) {
@@ -83,44 +96,53 @@ __global__ void k_from_dd(int64_t n, const double* __restrict__ src, double* __r
     }
 }
 
-Ptr36 pack8(const void* base, int64_t S) {
-    Ptr36 P;
-    for (int a = 0; a < 36; ++a) P.p[a] = static_cast<const char*>(base) + (size_t)a * S * 8;
-    return P;
+
+// One stage: the whole stage with beta terms, else its two halves.
+template <int STAGE, bool BETA, int REG>
+void stage_dd(const dim3& gr, const dim3& bl, cudaStream_t st, const Grid& g, const float2* X, const float2* y,
+              float2* yn, float2* xn, float2* acc_out, const PhysCoef<dd>& pc, const StencilCoef<dd>& sc, dd w,
+              dd h, float2* cur) {
+    const Ptr36 P = pack8(X, g.S);
+    if constexpr (BETA) {
+        k_stage_dd<STAGE, true, REG, 0><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
+    } else {
+        k_stage_dd<STAGE, false, REG, 1><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
+        k_stage_dd<STAGE, false, REG, 2><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
+    }
 }
 
 template <bool BETA, int REG>
 void step_dd(const Grid& g, const Tiling& t, float2* y, float2* yn, float2* xa, float2* xb, const PhysCoef<dd>& pc,
-             const StencilCoef<dd>& sc, double dt, cudaStream_t st) {
+             const StencilCoef<dd>& sc, double dt, float2* cur, cudaStream_t st) {
     const dim3 gr((g.nx + t.bx - 1) / t.bx, (g.ny + t.by - 1) / t.by, g.nz), bl(t.bx, t.by);
     const dd w6(dt / 6.), w3(dt / 3.), h2(dt / 2.), h1(dt), z(0.0);
-    k_stage_dd<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(y, g.S), y, yn, xa, nullptr, pc, sc, w6, h2);
-    k_stage_dd<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xa, g.S), y, yn, xb, nullptr, pc, sc, w3, h2);
-    k_stage_dd<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xb, g.S), y, yn, xa, nullptr, pc, sc, w3, h1);
-    k_stage_dd<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack8(xa, g.S), y, yn, nullptr, y, pc, sc, w6, z);
+    stage_dd<1, BETA, REG>(gr, bl, st, g, y, y, yn, xa, nullptr, pc, sc, w6, h2, cur);
+    stage_dd<2, BETA, REG>(gr, bl, st, g, xa, y, yn, xb, nullptr, pc, sc, w3, h2, cur);
+    stage_dd<3, BETA, REG>(gr, bl, st, g, xb, y, yn, xa, nullptr, pc, sc, w3, h1, cur);
+    stage_dd<4, BETA, REG>(gr, bl, st, g, xa, y, yn, nullptr, y, pc, sc, w6, z, cur);
 }
 
 template <bool BETA>
 void step_dd_r(const Grid& g, const Tiling& t, float2* y, float2* yn, float2* xa, float2* xb, const PhysCoef<dd>& pc,
-               const StencilCoef<dd>& sc, double dt, cudaStream_t st) {
+               const StencilCoef<dd>& sc, double dt, float2* cur, cudaStream_t st) {
     // the 128-register variant spills heavily in this form and runs as variant 0
     if (t.reg == 2)
-        step_dd<BETA, 2>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+        step_dd<BETA, 2>(g, t, y, yn, xa, xb, pc, sc, dt, cur, st);
     else
-        step_dd<BETA, 0>(g, t, y, yn, xa, xb, pc, sc, dt, st);
+        step_dd<BETA, 0>(g, t, y, yn, xa, xb, pc, sc, dt, cur, st);
 }
 
 }  // namespace
 
 cudaError_t launch_step_dd(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
-                           const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+                           double* cur, const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
     const PhysCoef<dd> pc = make_phys<dd>(p, Jex, gam);
     const StencilCoef<dd> sc = make_stencil<dd>(p.dx);
     auto f2p = [](double* v) { return reinterpret_cast<float2*>(v); };
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_dd_r<true>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, st);
+        step_dd_r<true>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, f2p(cur), st);
     else
-        step_dd_r<false>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, st);
+        step_dd_r<false>(g, t, f2p(y), f2p(yn), f2p(xa), f2p(xb), pc, sc, p.dt, f2p(cur), st);
     return cudaGetLastError();
 }
 

@@ -122,7 +122,7 @@ int ewpt_create(const ewpt_params* p, ewpt_ctx** out) {
         if (e == cudaSuccess) e = cudaMalloc(&c->yn, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->xa, n * 8);
         if (e == cudaSuccess) e = cudaMalloc(&c->xb, n * 8);
-        if (e == cudaSuccess && p->precision == EWPT_DF64) e = cudaMalloc(&c->ddcur, (size_t)9 * c->g.S * 8);
+        if (e == cudaSuccess && p->precision == EWPT_DF64) e = cudaMalloc(&c->ddcur, (size_t)12 * c->g.S * 8);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->y, 0, n * 8, c->st);
     } else {
         // ghosted layout; zero everything so the ghost cells no kernel writes

@@ -17,8 +17,8 @@ struct ewpt_ctx {
     double* yn = nullptr;
     double* xa = nullptr;
     double* xb = nullptr;
-    // DF64 form: [9][S] float pairs passing the Higgs current between the two
-    // launches of a stage (stage_dd.cu)
+    // DF64 form: [12][S] float pairs passing the Higgs currents between the
+    // launches of a split stage (stage_dd.cu)
     double* ddcur = nullptr;
     // FP32 form: compensated state, weighted rate sum, float stage inputs
     Fp32State y32{nullptr, nullptr};  // all five FP32 buffers: [36][lay.P]

@@ -31,11 +31,13 @@
 //   div3(a)                        dx(a) + dy(a+1) + dz(a+2)
 // Sink `out(a, rate)` receives rate a = d y_a / dt exactly once.
 //
-// PART splits the work between two launches when there are no beta terms:
-// 0 = everything; 1 = the field, auxiliary, Higgs and U(1) rates (0-23,
-// 33-35), handing the Higgs current of kt W to the sink
-// (out.keep_current(3 a + i, J^a_i)); 2 = the SU(2) rates (24-32), taking
-// that current back (out.load_current).  The values are those of PART 0.
+// PART splits the work between three launches when there are no beta terms:
+// 0 = everything; 1 = the Higgs rates (20-23), handing the Higgs currents of
+// kt W and kt Y to the sink (out.keep_current(3 a + i, J^a_i), slots 0-8;
+// out.keep_current(9 + i, J^Y_i), slots 9-11); 2 = the SU(2) rates (24-32);
+// 3 = the field, auxiliary and U(1) rates (0-19, 33-35).  Parts 2 and 3
+// take the currents back (out.load_current).  The values are those of
+// PART 0.
 #pragma once
 
 template <typename T>
@@ -61,7 +63,8 @@ __device__ __forceinline__ void cov_deriv(T d1, T d2, T d3, T d4, T p1, T p2, T 
 template <typename T, bool BETA, class Acc, class Sink, int PART = 0>
 __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
     static_assert(PART == 0 || !BETA, "the beta terms couple every block: PART 0 only");
-    constexpr bool kFirst = PART != 2, kSecond = PART != 1;
+    constexpr bool kHiggs = PART == 0 || PART == 1, kSU2 = PART == 0 || PART == 2,
+                   kRest = PART == 0 || PART == 3;
     const T gw = c.gw, gy = c.gy, hgw = c.hgw, hgy = c.hgy;
     const T p1 = A.v(0), p2 = A.v(1), p3 = A.v(2), p4 = A.v(3);
     T W[3][3];  // W[a][i] = W_{a+1}_{i+2}
@@ -75,13 +78,13 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     const T pt1 = A.v(20), pt2 = A.v(21), pt3 = A.v(22), pt4 = A.v(23);
 
     // ---- k_field = momentum (main_rk4.jl:585-600)
-    if constexpr (kFirst) {
+    if constexpr (kRest) {
 #pragma unroll
         for (int a = 0; a < 16; ++a) out(a, A.v(20 + a));
     }
 
     // ---- k_Gamma_a, k_Sigma (main_rk4.jl:603-655)
-    if constexpr (kFirst) {
+    if constexpr (kRest) {
         T Wt[3][3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -107,11 +110,17 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     T ktp1, ktp2, ktp3, ktp4;
     T jW[3][3], jY[3];
     T cx = T(0), cy = T(0), cz = T(0), pdot = T(0);
-    if constexpr (!kFirst) {
+    if constexpr (!kHiggs) {
+        if constexpr (kSU2) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+            for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) jW[a][i] = out.load_current(3 * a + i);
+                for (int i = 0; i < 3; ++i) jW[a][i] = out.load_current(3 * a + i);
+        }
+        if constexpr (kRest) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) jY[i] = out.load_current(9 + i);
+        }
     } else {
         T d1[3], d2[3], d3[3], d4[3], l1, l2, l3, l4;
         A.grad_lap(0, d1[0], d1[1], d1[2], l1);
@@ -157,6 +166,8 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
             for (int a = 0; a < 3; ++a)
 #pragma unroll
                 for (int i = 0; i < 3; ++i) out.keep_current(3 * a + i, jW[a][i]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) out.keep_current(9 + i, jY[i]);
         }
         if (BETA) {
             pdot = pt1 * p1 + pt2 * p2 + pt3 * p3 + pt4 * p4;
@@ -169,7 +180,7 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
     // ---- SU(2) block, one colour at a time (field_strengths.jl:34-224)
     T ktW[3][3];
     T F[3][3];  // F[b][0] = F^b_xy (W_b_23), [1] = F^b_xz (W_b_24), [2] = F^b_yz (W_b_34)
-    if constexpr (kSecond) {
+    if constexpr (kSU2) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
@@ -221,7 +232,7 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
 
     // ---- U(1) block (field_strengths.jl:281-311, main_rk4.jl:562-581)
     T ktY[3], FY[3];
-    if constexpr (kFirst) {
+    if constexpr (kRest) {
         T dY[3][3], lap[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) A.grad_lap(13 + i, dY[i][0], dY[i][1], dY[i][2], lap[i]);
@@ -264,19 +275,19 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         ktY[1] += byp * FY[1] + c.bY2 * (cz * Yt2 - cx * Yt4);
         ktY[2] += -byp * FY[0] + c.bY2 * (cx * Yt3 - cy * Yt2);
     }
-    if constexpr (kFirst) {
+    if constexpr (kHiggs) {
         out(20, ktp1);
         out(21, ktp2);
         out(22, ktp3);
         out(23, ktp4);
     }
-    if constexpr (kSecond) {
+    if constexpr (kSU2) {
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int i = 0; i < 3; ++i) out(24 + 3 * a + i, ktW[a][i]);
     }
-    if constexpr (kFirst) {
+    if constexpr (kRest) {
         out(33, ktY[0]);
         out(34, ktY[1]);
         out(35, ktY[2]);

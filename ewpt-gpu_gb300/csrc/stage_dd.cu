@@ -40,7 +40,7 @@ struct DdSink {
     float2* acc_out;
     int64_t S;
     dd w, h;
-    float2* cur;  // [9][S] Higgs current of kt W, from the first to the second launch of a split stage
+    float2* cur;  // [12][S] Higgs currents of kt W and kt Y, from the first launch of a split stage to the others
     __device__ __forceinline__ void keep_current(int q, dd v) const { cur[q * S + A.c] = v.f2(); }
     __device__ __forceinline__ dd load_current(int q) const { return dd(__ldg(cur + q * S + A.c)); }
     __device__ __forceinline__ void operator()(int a, dd r) const {
@@ -65,9 +65,11 @@ Ptr36 pack8(const void* base, int64_t S) {
     return P;
 }
 
-// PART (site_rates): 0 the whole stage; 1 and 2 its two halves, launched one
-// after the other when there are no beta terms -- each half is about half
-// of the straight-line code, which is what limits this form.
+// PART (site_rates): 0 the whole stage; 1-3 its three parts (Higgs; SU(2);
+// fields, auxiliaries and U(1)), launched one after the other when there
+// are no beta terms.  The double-float stage is instruction-fetch bound
+// (~20 k straight-line instructions per site): each part is a third of the
+// code, and the stencil routines are shared out-of-line calls.
 template <int STAGE, bool BETA, int REG, int PART>
 __global__ void __launch_bounds__(DdBudget<REG>::kThreads, DdBudget<REG>::kMinBlocks)
     k_stage_dd(Grid g, const __grid_constant__ Ptr36 X, const float2* __restrict__ y, float2* yn,
@@ -108,6 +110,7 @@ void stage_dd(const dim3& gr, const dim3& bl, cudaStream_t st, const Grid& g, co
     } else {
         k_stage_dd<STAGE, false, REG, 1><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
         k_stage_dd<STAGE, false, REG, 2><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
+        k_stage_dd<STAGE, false, REG, 3><<<gr, bl, 0, st>>>(g, P, y, yn, xn, acc_out, pc, sc, w, h, cur);
     }
 }
 

@@ -135,3 +135,17 @@ def test_thermal_ic_rejects_bad_arguments():
                 lat.init_thermal(*args)
         with pytest.raises(ewpt.EwptError):
             lat.init_thermal(1.5, mH=-1.0)
+
+
+def test_thermal_ic_uses_the_context_stencil():
+    """Gamma and Sigma are the divergences with the context's stencil order:
+    with the 8th-order stencil the constraint columns of the (8th-order)
+    snapshot row vanish too."""
+    p = ewpt.baseline_couplings(shape=(20, 18, 22), N=20, dx=0.25, dt=0.025, stencil_order=8)
+    with ewpt.Lattice(p) as lat:
+        lat.init_thermal(T, seed=5)
+        y = lat.get_state()
+        d = lat.diagnostics()
+    g_norm = math.sqrt((y[16:19] ** 2).sum() * p.dx ** 3)
+    s_norm = math.sqrt((y[19] ** 2).sum() * p.dx ** 3)
+    assert d[18] < 1e-12 * g_norm and d[19] < 1e-12 * s_norm

@@ -74,15 +74,23 @@ def time_tiling(lat: Lattice, tile, steps: int = 2) -> float:
     return e0.elapsed_time(e1) / 1e3 / steps
 
 
+def candidates_for(p: Params) -> list:
+    """The launch shapes offered for this lattice and form: the one-site
+    shapes always; for the FP32 form the paired shapes (even nx) and the
+    TMA-staged tiles (nx a multiple of 32, ny and nz multiples of the tile)."""
+    candidates = list(CANDIDATES)
+    nx, ny, nz = p.dims
+    if int(p.precision) == _lib.FP32 and nx % 2 == 0:
+        candidates += PAIR_CANDIDATES
+    if int(p.precision) == _lib.FP32 and nx % 32 == 0:
+        candidates += [t for t in TMA_CANDIDATES if ny % t[1] == 0 and nz % t[2] == 0]
+    return candidates
+
+
 def sweep(p: Params, steps: int = 2, candidates=None) -> list:
     """(tiling, seconds per step) for every candidate on a scratch lattice."""
     if candidates is None:
-        candidates = list(CANDIDATES)
-        if int(p.precision) == _lib.FP32 and p.dims[0] % 2 == 0:
-            candidates += PAIR_CANDIDATES
-        nx, ny, nz = p.dims
-        if int(p.precision) == _lib.FP32 and nx % 32 == 0:
-            candidates += [t for t in TMA_CANDIDATES if ny % t[1] == 0 and nz % t[2] == 0]
+        candidates = candidates_for(p)
     res = []
     with Lattice(p) as lat:
         R, w = ic.tanh_profile_params(p.lam, p.vev)

@@ -69,3 +69,25 @@ def test_cadence_parameters():
     assert p.dsnaps == 100 and p.dsnaps_fft == 40 and p.spec_cut == (64, 64, 64)
     q = ewpt.Params.from_args(["0.0", "10", "30", "0.25", "10", "32", "0.99", "4", "0.0", "0.0", "0.0", "1"])
     assert q.dsnaps == 7 and q.dsnaps_fft == 1  # floor(30/50) = 0 -> every snapshot
+
+
+def test_surrogate_parameter_draws():
+    """Seeded draws: features (lambda, g, g', bubble count[, T][, log2 N]);
+    thermal runs carry bubble count 0 and T in [1, 2]; a single size keeps
+    the four-feature layout."""
+    import numpy as np
+
+    from ewpt import surrogate
+
+    ps, prm, nb = surrogate.draw_members(200, [64, 96, 128], seed=3, thermal_fraction=0.5)
+    assert prm.shape == (200, 6) and len(ps) == 200
+    th = prm[:, 4] > 0
+    assert 60 < th.sum() < 140
+    assert (prm[th, 3] == 0).all() and (nb[th] == 0).all() and ((prm[th, 4] >= 1) & (prm[th, 4] <= 2)).all()
+    assert (prm[~th, 3] >= 4).all() and (prm[~th, 3] <= 16).all()
+    assert set(prm[:, 5]) <= {6.0, np.log2(96), 7.0}
+    assert [p.dims[0] for p in ps] == [int(round(2 ** v)) for v in prm[:, 5]]
+    ps2, prm2, _ = surrogate.draw_members(200, [64, 96, 128], seed=3, thermal_fraction=0.5)
+    np.testing.assert_array_equal(prm, prm2)
+    _, prm1, _ = surrogate.draw_members(10, 24, seed=1)
+    assert prm1.shape == (10, 4)

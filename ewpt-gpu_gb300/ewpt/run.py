@@ -1,7 +1,7 @@
 """Driver with the reference's command-line and output cadence.
 
     python -m ewpt.run gamma no_bubbles nte dx dtdiv N gp2 nsnaps T beta_Y beta_W seed \\
-        [--thermal] [--fp32] [--out DIR] [--nshell 40] [--fft-dumps]
+        [--thermal] [--fp32 | --df64] [--out DIR] [--nshell 40] [--fft-dumps]
 
 Mirrors run() of gpu-kernels-rk4/main_rk4.jl:5174-7081 on top of libewpt:
 parameters from the 12 positional ARGS (parameters.jl:14-55), a bubble
@@ -197,11 +197,14 @@ def main(argv=None):
     ap.add_argument("args", nargs=12, help="gamma no_bubbles nte dx dtdiv N gp2 nsnaps T beta_Y beta_W seed")
     ap.add_argument("--thermal", action="store_true", help="thermal IC and the J_ext/damp schedule")
     ap.add_argument("--fp32", action="store_true", help="FP32 stencil/flux form")
+    ap.add_argument("--df64", action="store_true", help="double-float form (the FP64 scheme on the FP32 pipes)")
     ap.add_argument("--out", default=None)
     ap.add_argument("--nshell", type=int, default=40)
     ap.add_argument("--fft-dumps", action="store_true", help="3d-fft-data-<it>.npz B / B_2 FFT dumps")
     a = ap.parse_args(argv)
-    p = Params.from_args(a.args, precision=_lib.FP32 if a.fp32 else _lib.FP64)
+    if a.fp32 and a.df64:
+        ap.error("--fp32 and --df64 exclude each other")
+    p = Params.from_args(a.args, precision=_lib.FP32 if a.fp32 else _lib.DF64 if a.df64 else _lib.FP64)
     res = run(p, thermal_init=a.thermal, out_dir=a.out, nshell=a.nshell, fft_dumps=a.fft_dumps)
     print(f"done: {res['iterations']} RK4 steps in {res['seconds']:.2f} s")
 

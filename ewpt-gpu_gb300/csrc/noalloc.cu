@@ -8,18 +8,17 @@
 // must not hit the driver's allocator in the middle of a time-critical loop.
 // This variant keeps its scratch in a fixed file-scope device array instead.
 //
-// The array is sized for EWPT_NOALLOC_MAX_TILES partial rows, one per
-// 32x4-site x-y tile of the lattice, plus the final row.  Every GPU that
-// loads the library holds it until the process exits (about 0.7 MB).
-// Calls share the array: two calls whose kernels overlap on the GPU (on
-// different streams, or from different host threads) race on it.
+// The array is sized for EWPT_NOALLOC_MAX_TILES partial rows of kRowLen
+// doubles, one row per 32x4-site x-y tile of the lattice, plus the final
+// row: (4096 * 32 + 32) * 8 = 1,048,832 bytes.  Every GPU that loads the
+// library holds it until the process exits.  Calls share the array: two
+// calls whose kernels overlap on the GPU (on different streams, or from
+// different host threads) race on it.
 #include <cstdio>
-#include <mutex>
 
 #include "ewpt_ctx.cuh"
 
 #define EWPT_NOALLOC_MAX_TILES 4096
-#define EWPT_NOALLOC_MAX_DEVICES 64
 
 cudaError_t launch_diag_bounded(const Grid& g, const ewpt_params& p, const double* y, double* part,
                                 int64_t max_rows, double* dres, cudaStream_t st);
@@ -36,25 +35,42 @@ constexpr int64_t kScratch = (int64_t)EWPT_NOALLOC_MAX_TILES * kRowLen + kRowLen
 // symbol: its device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) double g_noalloc_scratch[kScratch];
 
-std::mutex g_mu;
-double* g_addr[EWPT_NOALLOC_MAX_DEVICES] = {};
-
-// Device address of the scratch on `dev`, looked up once per device with that
-// device current.
+// Device address of the scratch on the current device.  Looked up on every
+// call (it is not a stream operation and costs microseconds): a cached
+// address would go stale if the caller reset the device or tore down its
+// primary context, which reloads the module at a new address.
 int scratch_address(int dev, double** out) {
-    if (dev < 0 || dev >= EWPT_NOALLOC_MAX_DEVICES)
-        return ewpt_fail(nullptr, EWPT_ERR_ARG, "device %d beyond the %d devices this entry point supports", dev,
-                         EWPT_NOALLOC_MAX_DEVICES);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        double* ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            return ewpt_fail(nullptr, EWPT_ERR_CUDA, "cudaGetSymbolAddress(noalloc scratch) on device %d: %s", dev,
-                             cudaGetErrorString(e));
-        g_addr[dev] = ptr;
-    }
-    *out = g_addr[dev];
+    double* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return ewpt_fail(nullptr, EWPT_ERR_CUDA, "cudaGetSymbolAddress(noalloc scratch) on device %d: %s", dev,
+                         cudaGetErrorString(e));
+    *out = ptr;
+    return EWPT_OK;
+}
+
+// The diagnostics on the current device (the caller's device is restored by
+// the entry point below).
+int diagnostics_noalloc_on(const ewpt_params* p, const Grid& g, const double* state, double* out, cudaStream_t st) {
+    double* scratch = nullptr;
+    int rc = scratch_address(p->device, &scratch);
+    if (rc) return rc;
+    double* part = scratch;
+    double* res = scratch + (int64_t)EWPT_NOALLOC_MAX_TILES * kRowLen;
+    // Every block writes its whole partial row and the final kernel reads
+    // only those rows, so what an earlier call left in the array is never
+    // read and nothing needs clearing.
+    cudaError_t e =
+        launch_diag_bounded(g, *p, state, part, (int64_t)EWPT_NOALLOC_MAX_TILES * kRowLen / diag_nred(), res, st);
+    double r[kRowLen];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r, res, (size_t)diag_nred() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    rc = ewpt_cuda_check(nullptr, e, "diagnostics_noalloc");
+    if (rc) return rc;
+    diag_finish_row(*p, g.S, r, out);
+    for (int q = 0; q < EWPT_NDIAG; ++q)
+        if (!(out[q] == out[q]) || out[q] - out[q] != 0.0)
+            return ewpt_fail(nullptr, EWPT_ERR_NONFINITE, "non-finite diagnostic column %d", q);
     return EWPT_OK;
 }
 
@@ -73,25 +89,15 @@ extern "C" int ewpt_diagnostics_noalloc(const ewpt_params* p, const double* stat
                          "lattice %dx%d needs %lld x-y tiles of 32x4 sites; ewpt_diagnostics_noalloc holds at most %d "
                          "(use ewpt_diagnostics for larger lattices)",
                          p->nx, p->ny, (long long)tiles, EWPT_NOALLOC_MAX_TILES);
-    cudaError_t e = cudaSetDevice(p->device);
+    // the caller's current device is put back on every path below: a Julia
+    // or PyTorch host thread keeps the device it had chosen
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) return ewpt_cuda_check(nullptr, e, "noalloc get device");
+    e = cudaSetDevice(p->device);
     if (e != cudaSuccess) return ewpt_cuda_check(nullptr, e, "noalloc set device");
-    double* scratch = nullptr;
-    rc = scratch_address(p->device, &scratch);
-    if (rc) return rc;
-    const cudaStream_t st = (cudaStream_t)stream;
-    double* part = scratch;
-    double* res = scratch + (int64_t)EWPT_NOALLOC_MAX_TILES * kRowLen;
-    // Stride of the partial rows is the kernel's own row length; rows beyond
-    // the ones this call writes are never read, so nothing needs clearing.
-    e = launch_diag_bounded(g, *p, state, part, (int64_t)EWPT_NOALLOC_MAX_TILES * kRowLen / diag_nred(), res, st);
-    double r[kRowLen];
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r, res, (size_t)diag_nred() * sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    rc = ewpt_cuda_check(nullptr, e, "diagnostics_noalloc");
-    if (rc) return rc;
-    diag_finish_row(*p, g.S, r, out);
-    for (int q = 0; q < EWPT_NDIAG; ++q)
-        if (!(out[q] == out[q]) || out[q] - out[q] != 0.0)
-            return ewpt_fail(nullptr, EWPT_ERR_NONFINITE, "non-finite diagnostic column %d", q);
-    return EWPT_OK;
+    rc = diagnostics_noalloc_on(p, g, state, out, (cudaStream_t)stream);
+    e = cudaSetDevice(prev);
+    if (rc == EWPT_OK && e != cudaSuccess) rc = ewpt_cuda_check(nullptr, e, "noalloc restore device");
+    return rc;
 }

@@ -283,11 +283,14 @@ int ewpt_mlp_train_step(ewpt_mlp* net, const float* x, const float* y, int32_t b
  * fixed.  `state` is a device pointer to 36*nx*ny*nz doubles in the order
  * above (packed, array-major); `out` is host memory; work is queued on
  * `stream` (a cudaStream_t or NULL) and the call waits for it.
- * Scratch lives in one fixed device array per GPU (about 0.7 MB, held until
- * the process exits), sized for at most 4096 x-y tiles of 32x4 sites
+ * Scratch lives in one fixed device array per GPU (1,048,832 bytes: 4096
+ * partial rows of 32 doubles plus the final row, held until the process
+ * exits), sized for at most 4096 x-y tiles of 32x4 sites
  * (ceil(nx/32)*ceil(ny/4) <= 4096, e.g. nx = ny = 512); larger lattices are
- * rejected with EWPT_ERR_ARG.  The first call on each device looks up the
- * array's device address; make that first call before any stream capture.
+ * rejected with EWPT_ERR_ARG.  Each call looks up the array's device address
+ * on p->device and restores the caller's current device before it returns.
+ * The call copies the row into host memory and waits for its stream, so it
+ * must not be called while that stream is being captured into a CUDA graph.
  * Calls share the array and each one overwrites it: calls whose work
  * overlaps on the GPU race and must be serialised by the caller. */
 int ewpt_diagnostics_noalloc(const ewpt_params* p, const double* state, double out[EWPT_NDIAG], void* stream);

@@ -4,6 +4,12 @@ device memory is already owned by another allocator's pool).  It must give
 the same snapshot row as ewpt_diagnostics, call after call, although its
 scratch array keeps whatever the previous call left in it.
 
+The lattices cover the small case (one reduction block per x-y tile and z
+plane), lattices whose z planes fold into each block's loop (256x256x64:
+512 tiles, each block walks ~21 planes; 512x512x10 with the 8th-order
+stencil: 2048 tiles, one block per tile walks all 10 planes), and the
+largest accepted x-y extent (1024x512: exactly 4096 tiles).
+
 This file is named so that pytest collects it last; it passes both alone in
 a fresh process and after the other tests."""
 import ctypes as C
@@ -41,21 +47,31 @@ def built():
     build_lib.build()
 
 
-def test_noalloc_matches_diagnostics_on_two_calls_in_a_row():
+@pytest.mark.parametrize("shape,order,side_stream", [
+    ((40, 36, 24), 6, False),
+    ((256, 256, 64), 6, True),
+    ((512, 512, 10), 8, False),
+    ((1024, 512, 8), 6, True),
+])
+def test_noalloc_matches_diagnostics_on_two_calls_in_a_row(shape, order, side_stream):
     import torch
 
-    shape = (40, 36, 24)
-    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025)
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025, stencil_order=order)
     states = [_state(shape, 3), _state(shape, 4)]
     refs = []
     with ewpt.Lattice(p) as lat:
         for y in states:
             lat.set_state(y)
             refs.append(lat.diagnostics())
+    stream = torch.cuda.Stream() if side_stream else torch.cuda.current_stream()
+    dev_before = torch.cuda.current_device()
     for y, ref in zip(states, refs):
-        dev = torch.tensor(y, dtype=torch.float64, device="cuda:0").contiguous()
-        got = _noalloc(p, dev.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        with torch.cuda.stream(stream):
+            dev = torch.tensor(y, dtype=torch.float64, device="cuda:0").contiguous()
+        got = _noalloc(p, dev.data_ptr(), stream.cuda_stream)
         np.testing.assert_allclose(got, ref, rtol=RTOL, atol=1e-13)
+        del dev
+    assert torch.cuda.current_device() == dev_before
     assert not np.allclose(refs[0], refs[1])
 
 

@@ -12,13 +12,17 @@ lattice and reported in the same line.
 
 value    FP64 site-updates/s with the state resident in HBM (CUDA events on
          the library's stream; the 4.8 GB state is larger than L2).
-e2e      the same metric through the C ABI with host buffers: every step
-         uploads the state from pinned host memory (ewpt_set_state_packed),
-         steps once (ewpt_step) and reads the energy row back
-         (ewpt_diagnostics).
+e2e      the same metric through the C ABI with host buffers, as a drop-in
+         rk4_step! caller sees it: every step uploads the state from pinned
+         host memory (ewpt_set_state_packed), steps once (ewpt_step), reads
+         the evolved state back into pinned host memory
+         (ewpt_get_state_packed) and the snapshot row (ewpt_diagnostics).
 roofline HBM roofline of the stage kernels: algorithmic bytes per
          site-update (3744 B FP64, 2592 B FP32 form) x site-updates/s over
          the measured copy bandwidth.
+roofline_compute  the FP64 form's own bound, the FP64 pipe: counted FLOPs
+         per site-update x site-updates/s over the FP64 peak measured in
+         this run (ewpt_fp64_peak, fused multiply-add chains on every SM).
 --impl reference  times the CPU restatement of the reference's routines (the
          oracle) on the host cores on a bounded sample lattice.
 With --gpus N > 1 (torchrun), each rank evolves its own replica; value is the
@@ -48,6 +52,13 @@ BYTES_FP32 = 2592  # y in FP64 width, stage rates in FP32
 # so a 256^3 launch moves this x S / 4.
 TRAFFIC_FP64 = 4383
 TRAFFIC_FP32 = 2804
+# FP64 operations of one site-update of the FP64 stage kernels (4 stages of
+# site_rates + the RK4 epilogue), counted exactly by compiling the kernels'
+# own per-site templates with an operator-counting scalar type
+# (tests/test_devphys.py checks these figures against that count): FLOPs with
+# an FMA as 2, and FP64 pipe instructions with single-use products fused.
+FLOPS_FP64 = 7300
+FP64_INST_EST = 4976
 N_BUBBLES = 64
 
 
@@ -189,12 +200,13 @@ def run_ours(args, ws, rank, local):
         t = allmax(ws, t)
         clocks = ck.summary()
         d = lat.diagnostics()
-        res["fp64"] = dict(t=t, diag=d.tolist())
+        res["fp64"] = dict(t=t, diag=d.tolist(), peak=ewpt._lib.fp64_peak(local))
         # ------------------------------------------------------------ e2e
         if not args.no_e2e:
             host = torch.empty((36, S), dtype=torch.float64, pin_memory=True)
             host.numpy()[:] = y0
-            ptr = host.data_ptr()
+            back = torch.empty((36, S), dtype=torch.float64, pin_memory=True)
+            ptr, bptr = host.data_ptr(), back.data_ptr()
             row = np.zeros(20)
             L = lat.L
             import ctypes as C
@@ -202,17 +214,18 @@ def run_ours(args, ws, rank, local):
             def e2e_step():
                 ewpt._lib.check(L.ewpt_set_state_packed(lat.h, C.c_void_p(ptr), 0), lat.h)
                 ewpt._lib.check(L.ewpt_step(lat.h, 1), lat.h)
+                ewpt._lib.check(L.ewpt_get_state_packed(lat.h, C.c_void_p(bptr), 0), lat.h)
                 ewpt._lib.check(L.ewpt_diagnostics(lat.h, row.ctypes.data_as(ewpt._lib.DP)), lat.h)
 
             for _ in range(max(1, min(args.warmup, 2))):
                 e2e_step()
-            ke = max(1, min(args.steps, 5))
+            ke = max(1, args.steps)
             barrier(ws)
             t0 = time.perf_counter()
             for _ in range(ke):
                 e2e_step()
             te = allmax(ws, time.perf_counter() - t0)
-            res["e2e"] = dict(t=te, steps=ke, h2d=36 * S * 8, d2h=20 * 8)
+            res["e2e"] = dict(t=te, steps=ke, h2d=36 * S * 8, d2h=36 * S * 8 + 20 * 8)
     # ---------------------------------------------------------------- FP32
     if not args.no_fp32:
         p32 = make_params(n, ewpt.FP32)
@@ -274,7 +287,17 @@ def run_ours(args, ws, rank, local):
                      "launch_ms": t64 / args.steps / 4 * 1e3,
                      "traffic_source": "ncu dram bytes per site-update at 80^3 x sites / 4",
                      "algorithmic_bytes_per_site_update": BYTES_FP64,
-                     "note": "FP64 form is bound by the FP64 pipe (86% busy), not HBM"},
+                     "limiter": "the FP64 pipe, not HBM: see roofline_compute"},
+        "roofline_compute": {"bound": "fp64", "achieved": S * args.steps / t64 * FLOPS_FP64 / 1e12,
+                             "peak": res["fp64"]["peak"] / 1e12, "unit": "TFLOP/s",
+                             "frac": S * args.steps / t64 * FLOPS_FP64 / res["fp64"]["peak"],
+                             "peak_kind": "measured in this run: ewpt_fp64_peak (DFMA chains on every SM)",
+                             "flops_per_site_update": FLOPS_FP64,
+                             "flops_source": "exact count of the kernels' per-site source (oracle/devphys.cu), "
+                                             "FMA = 2 FLOPs",
+                             "fp64_inst_per_site_update_est": FP64_INST_EST,
+                             "pipe_frac_est": S * args.steps / t64 * FP64_INST_EST / (res["fp64"]["peak"] / 2),
+                             "kernel": "k_stage_fp64 (4 launches/step)"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
     }
@@ -282,7 +305,8 @@ def run_ours(args, ws, rank, local):
         e = res["e2e"]
         out["e2e"] = {"value": ws * S * e["steps"] / e["t"], "unit": "site-updates/s",
                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
-                      "path": "ewpt_set_state_packed(pinned host) + ewpt_step(1) + ewpt_diagnostics per step"}
+                      "path": "ewpt_set_state_packed(pinned host) + ewpt_step(1) + "
+                              "ewpt_get_state_packed(pinned host) + ewpt_diagnostics per step"}
     if "fp32" in res:
         f = res["fp32"]
         v32 = ws * S * f["steps"] / f["t"]
@@ -394,7 +418,11 @@ def cpu_baseline(budget_s=20.0, threads=None):
 
 
 def run_reference(args, ws, rank):
-    """CPU reference arm: the oracle on all host cores, bounded sample."""
+    """CPU reference arm: the oracle (the C restatement of rk4_step! and its
+    RK4 broadcasts) on all host cores.  It runs the full workload lattice
+    when W + K steps there fit in --ref-seconds (a 256^3 step takes ~5 s on
+    16 Arm cores); otherwise a smaller lattice with the same per-site work
+    stands in as the sample."""
     if rank != 0:
         return
     import numpy as np
@@ -404,28 +432,34 @@ def run_reference(args, ws, rank):
 
     orc.build()
     nthr = orc.num_threads()
-    # size the sample lattice so one step takes ~2 s on this host
-    probe = make_params(32, ewpt.FP64)
-    op = orc.params(probe.dims, probe.dx, probe.gw, probe.gy, probe.gp2, probe.lam, probe.vev)
-    y = ewpt.ic.bubbles_tanh(probe.dims, probe.dx, 4, seed=3)
-    t0 = time.perf_counter()
-    orc.rk4_step(op, y, probe.dt)
-    per_site = (time.perf_counter() - t0) / probe.sites
-    n = int(round((2.0 / max(per_site, 1e-12)) ** (1.0 / 3.0)))
-    n = max(32, min(args.n, (n // 8) * 8))
-    p = make_params(n, ewpt.FP64)
+    p = make_params(args.n, ewpt.FP64)
     op = orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
-    y = ewpt.ic.bubbles_tanh(p.dims, p.dx, max(4, N_BUBBLES * n ** 3 // args.n ** 3), seed=1234)
+    y = ewpt.ic.bubbles_tanh(p.dims, p.dx, N_BUBBLES, seed=1234)
     work = np.empty(3 * y.size)
-    for _ in range(args.warmup):
+    t0 = time.perf_counter()
+    y = orc.rk4_step(op, y, p.dt, work=work)  # first warm-up step, at the full workload
+    t1 = time.perf_counter() - t0
+    n = args.n
+    if (args.warmup - 1 + args.steps) * t1 > args.ref_seconds:
+        # sample lattice sized so that one step takes ~2 s
+        n = int(round((2.0 / t1) ** (1.0 / 3.0) * args.n))
+        n = max(32, min(args.n, (n // 8) * 8))
+        p = make_params(n, ewpt.FP64)
+        op = orc.params(p.dims, p.dx, p.gw, p.gy, p.gp2, p.lam, p.vev, p.beta_w, p.beta_y, p.theta_w)
+        y = ewpt.ic.bubbles_tanh(p.dims, p.dx, max(4, N_BUBBLES * n ** 3 // args.n ** 3), seed=1234)
+        work = np.empty(3 * y.size)
+        y = orc.rk4_step(op, y, p.dt, work=work)
+    for _ in range(args.warmup - 1):
         y = orc.rk4_step(op, y, p.dt, work=work)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         y = orc.rk4_step(op, y, p.dt, work=work)
     el = time.perf_counter() - t0
     v = p.sites * args.steps / el
-    sample = (f"{n}^3 sample lattice with the {args.n}^3 workload's per-site work (FP64 RK4 steps, "
-              f"64-bubble density), oracle C restatement of rk4_step! + RK4 broadcasts, OpenMP {nthr} threads")
+    same = n == args.n
+    sample = (f"{n}^3 lattice{' (the full workload)' if same else f' sample with the {args.n}^3 workload per-site work'}"
+              f", {N_BUBBLES if same else max(4, N_BUBBLES * n ** 3 // args.n ** 3)} tanh bubbles, {args.steps} "
+              f"FP64 RK4 steps of the oracle (C restatement of rk4_step! + RK4 broadcasts), OpenMP {nthr} threads")
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "site-updates/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -448,6 +482,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=300.0,
+                    help="reference arm: largest projected CPU time for W + K steps at the full lattice")
     ap.add_argument("--no-tune", action="store_true", help="keep the default 32x4 tiling")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-df64", action="store_true", help="skip the double-float form")

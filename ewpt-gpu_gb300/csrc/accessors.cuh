@@ -13,7 +13,7 @@
 template <typename TL>
 struct SrcPtr36 {
     const Ptr36& P;
-    __device__ __forceinline__ const TL* arr(int a) const { return reinterpret_cast<const TL*>(P.p[a]); }
+    EWPT_ARITH const TL* arr(int a) const { return reinterpret_cast<const TL*>(P.p[a]); }
 };
 
 template <typename TL>
@@ -39,18 +39,24 @@ struct SiteAcc {
     int ox[6], oy[6], oz[6];
     StencilCoef<T> s;
 
-    __device__ __forceinline__ T ld(int a, int off) const { return (T)__ldg(src.arr(a) + (c + off)); }
-    __device__ __forceinline__ T v(int a) const { return ld(a, 0); }
-    __device__ __forceinline__ T d1(int a, const int* o) const {
+    EWPT_ARITH T ld(int a, int off) const {
+#ifdef __CUDA_ARCH__
+        return (T)__ldg(src.arr(a) + (c + off));
+#else
+        return (T)src.arr(a)[c + off];
+#endif
+    }
+    EWPT_ARITH T v(int a) const { return ld(a, 0); }
+    EWPT_ARITH T d1(int a, const int* o) const {
         return s.a1 * (ld(a, o[0]) - ld(a, o[3])) + s.a2 * (ld(a, o[1]) - ld(a, o[4])) +
                s.a3 * (ld(a, o[2]) - ld(a, o[5]));
     }
-    __device__ __forceinline__ void grad(int a, T& gx, T& gy, T& gz) const {
+    EWPT_ARITH void grad(int a, T& gx, T& gy, T& gz) const {
         gx = d1(a, ox);
         gy = d1(a, oy);
         gz = d1(a, oz);
     }
-    __device__ __forceinline__ void grad_lap(int a, T& gx, T& gy, T& gz, T& lap) const {
+    EWPT_ARITH void grad_lap(int a, T& gx, T& gy, T& gz, T& lap) const {
         T s1, s2, s3;
         {
             const T p1 = ld(a, ox[0]), p2 = ld(a, ox[1]), p3 = ld(a, ox[2]);
@@ -78,7 +84,15 @@ struct SiteAcc {
         }
         lap = s.l0 * v(a) + s.l1 * s1 + s.l2 * s2 + s.l3 * s3;
     }
-    __device__ __forceinline__ T div3(int a) const { return d1(a, ox) + d1(a + 1, oy) + d1(a + 2, oz); }
+    // dx(a) + dy(a+1) + dz(a+2), the nine differences summed in one chain
+    EWPT_ARITH T div3(int a) const {
+        T r = s.a1 * (ld(a, ox[0]) - ld(a, ox[3]));
+        r = r + s.a2 * (ld(a, ox[1]) - ld(a, ox[4])) + s.a3 * (ld(a, ox[2]) - ld(a, ox[5]));
+        r = r + s.a1 * (ld(a + 1, oy[0]) - ld(a + 1, oy[3])) + s.a2 * (ld(a + 1, oy[1]) - ld(a + 1, oy[4])) +
+            s.a3 * (ld(a + 1, oy[2]) - ld(a + 1, oy[5]));
+        return r + s.a1 * (ld(a + 2, oz[0]) - ld(a + 2, oz[3])) + s.a2 * (ld(a + 2, oz[1]) - ld(a + 2, oz[4])) +
+               s.a3 * (ld(a + 2, oz[2]) - ld(a + 2, oz[5]));
+    }
 
     // site (i, j, k) of an nx x ny x nz box
     __device__ __forceinline__ void place(int i, int j, int k, int nx, int ny, int nz) {

@@ -59,6 +59,8 @@ int ewpt_validate_params(const ewpt_params* p, ewpt_ctx* ctx) {
     for (double x : v)
         if (!std::isfinite(x)) return ewpt_fail(ctx, EWPT_ERR_ARG, "non-finite parameter");
     if (!(p->dx > 0)) return ewpt_fail(ctx, EWPT_ERR_ARG, "dx must be > 0");
+    if (p->gw == 0.0)
+        return ewpt_fail(ctx, EWPT_ERR_ARG, "gw must be nonzero (the stage kernels sum the SU(2) terms over g)");
     if (!(p->dt > 0)) return ewpt_fail(ctx, EWPT_ERR_ARG, "dt must be > 0");
     return EWPT_OK;
 }

@@ -97,8 +97,9 @@ struct EnsSink {
 
 template <typename T>
 __device__ __forceinline__ PhysCoef<T> widen(const PhysCoef<float>& c) {
-    return PhysCoef<T>{T(c.gw),  T(c.gy),  T(c.hgw), T(c.hgy), T(c.gp2), T(c.omgp2), T(c.lam2),
-                       T(c.vev2), T(c.bW), T(c.bY), T(c.bW2), T(c.bY2), T(c.hJex), T(c.gam)};
+    return PhysCoef<T>{T(c.gw),   T(c.gy),    T(c.hgw),   T(c.hgy),   T(c.gp2),  T(c.omgp2), T(c.lam2),
+                       T(c.vev2), T(c.bW),    T(c.bY),    T(c.bW2),   T(c.bY2),  T(c.hJex),  T(c.gam),
+                       T(c.gg),   T(c.ggy),   T(c.lam2h), T(c.hJexh), T(c.gamh), T(c.ryw),   T(c.igw)};
 }
 
 template <int STAGE, bool BETA, bool PAIR>

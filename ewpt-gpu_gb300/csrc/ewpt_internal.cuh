@@ -110,6 +110,14 @@ PhysCoef<T> make_phys(const ewpt_params& p, double Jex, double gam) {
     c.bY2 = (T)(2.0 * p.beta_y);
     c.hJex = (T)(0.5 * Jex);
     c.gam = (T)gam;
+    // p.gw != 0 (ewpt_validate_params)
+    c.gg = (T)(p.gp2 * p.gw);
+    c.ggy = (T)(p.gp2 * p.gy);
+    c.lam2h = (T)(2.0 * p.lambda / (0.5 * p.gw));
+    c.hJexh = (T)(0.5 * Jex / (0.5 * p.gw));
+    c.gamh = (T)(gam / (0.5 * p.gw));
+    c.ryw = (T)(p.gy / p.gw);
+    c.igw = (T)(1.0 / p.gw);
     return c;
 }
 

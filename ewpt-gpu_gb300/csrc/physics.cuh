@@ -40,6 +40,14 @@
 // PART 0.
 #pragma once
 
+// Qualifier of the per-site arithmetic (here and in accessors.cuh).  The
+// library compiles it for the device only; the operation counter of the test
+// suite (oracle/opcount.cu) defines it as __host__ __device__ to run the same
+// templates on the host with an operator-counting scalar type.
+#ifndef EWPT_ARITH
+#define EWPT_ARITH __device__ __forceinline__
+#endif
+
 template <typename T>
 struct PhysCoef {
     T gw, gy, hgw, hgy;  // g, g', g/2, g'/2
@@ -47,12 +55,28 @@ struct PhysCoef {
     T lam2, vev2;        // 2*lambda, vev^2
     T bW, bY, bW2, bY2;  // beta_W, beta_Y, 2*beta_W, 2*beta_Y
     T hJex, gam;         // Jex/2, damping gamma
+    // derived, for rates accumulated in units of the couplings
+    T gg, ggy;           // gp2*g, gp2*g'
+    T lam2h, hJexh, gamh;// 2*lambda, Jex/2 and gamma over g/2
+    T ryw, igw;          // g'/g, 1/g
 };
 
 // Covariant derivatives D_i phi_a (cov_derivs_temporal.jl:23-130) along one
-// axis with gauge components W1 = W_1_i, W2 = W_2_i, W3 = W_3_i, Y = Y_i.
+// axis with gauge components W1 = W_1_i, W2 = W_2_i, W3 = W_3_i and the
+// hypercharge component in units of g: Yr = (g'/g) Y_i, so that
+// D = d + (g/2) (W terms + Yr terms).
 template <typename T>
-__device__ __forceinline__ void cov_deriv(T d1, T d2, T d3, T d4, T p1, T p2, T p3, T p4, T W1, T W2, T W3, T Y,
+EWPT_ARITH void cov_deriv_s(T d1, T d2, T d3, T d4, T p1, T p2, T p3, T p4, T W1, T W2, T W3, T Yr, T hgw, T& D1,
+                            T& D2, T& D3, T& D4) {
+    D1 = d1 + hgw * (W1 * p4 - W2 * p3 + W3 * p2 + Yr * p2);
+    D2 = d2 - hgw * (W1 * p3 + W2 * p4 + W3 * p1 + Yr * p1);
+    D3 = d3 + hgw * (W1 * p2 + W2 * p1 - W3 * p4 + Yr * p4);
+    D4 = d4 - hgw * (W1 * p1 - W2 * p2 - W3 * p3 + Yr * p3);
+}
+
+// The same with Y_i and g'/2 apart (the diagnostics).
+template <typename T>
+EWPT_ARITH void cov_deriv(T d1, T d2, T d3, T d4, T p1, T p2, T p3, T p4, T W1, T W2, T W3, T Y,
                                           T hgw, T hgy, T& D1, T& D2, T& D3, T& D4) {
     D1 = d1 + hgw * (W1 * p4 - W2 * p3 + W3 * p2) + hgy * (Y * p2);
     D2 = d2 - hgw * (W1 * p3 + W2 * p4 + W3 * p1) - hgy * (Y * p1);
@@ -61,11 +85,11 @@ __device__ __forceinline__ void cov_deriv(T d1, T d2, T d3, T d4, T p1, T p2, T 
 }
 
 template <typename T, bool BETA, class Acc, class Sink, int PART = 0>
-__device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
+EWPT_ARITH void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
     static_assert(PART == 0 || !BETA, "the beta terms couple every block: PART 0 only");
     constexpr bool kHiggs = PART == 0 || PART == 1, kSU2 = PART == 0 || PART == 2,
                    kRest = PART == 0 || PART == 3;
-    const T gw = c.gw, gy = c.gy, hgw = c.hgw, hgy = c.hgy;
+    const T gw = c.gw, gy = c.gy, hgw = c.hgw;
     const T p1 = A.v(0), p2 = A.v(1), p3 = A.v(2), p4 = A.v(3);
     T W[3][3];  // W[a][i] = W_{a+1}_{i+2}
 #pragma unroll
@@ -83,30 +107,33 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         for (int a = 0; a < 16; ++a) out(a, A.v(20 + a));
     }
 
-    // ---- k_Gamma_a, k_Sigma (main_rk4.jl:603-655)
+    // ---- k_Gamma_a, k_Sigma (main_rk4.jl:603-655): (1 - gp2) d_i pi^a_i + gp2 g rho^a
     if constexpr (kRest) {
         T Wt[3][3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int i = 0; i < 3; ++i) Wt[a][i] = A.v(24 + 3 * a + i);
-        const T gg = c.gp2 * gw;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const int b = (a + 1) % 3, cc = (a + 2) % 3;
-            // -((W_b . Wt_c) - (W_c . Wt_b)) summed over i, as written per i
-            T q = -(W[b][0] * Wt[cc][0] - W[cc][0] * Wt[b][0]) - (W[b][1] * Wt[cc][1] - W[cc][1] * Wt[b][1]) -
-                  (W[b][2] * Wt[cc][2] - W[cc][2] * Wt[b][2]);
-            T h;
-            if (a == 0) h = p1 * pt4 - p4 * pt1 + p3 * pt2 - p2 * pt3;
-            else if (a == 1) h = p3 * pt1 - p1 * pt3 + p4 * pt2 - p2 * pt4;
-            else h = p1 * pt2 - p2 * pt1 + p4 * pt3 - p3 * pt4;
-            out(16 + a, c.omgp2 * A.div3(24 + 3 * a) + gg * q + gg * h);
+            // Higgs charge, then the gauge charge -(W^b . Wt^c - W^c . Wt^b)
+            T q;
+            if (a == 0) q = p1 * pt4 - p4 * pt1 + p3 * pt2 - p2 * pt3;
+            else if (a == 1) q = p3 * pt1 - p1 * pt3 + p4 * pt2 - p2 * pt4;
+            else q = p1 * pt2 - p2 * pt1 + p4 * pt3 - p3 * pt4;
+            q = q - W[b][0] * Wt[cc][0] + W[cc][0] * Wt[b][0] - W[b][1] * Wt[cc][1] + W[cc][1] * Wt[b][1] -
+                W[b][2] * Wt[cc][2] + W[cc][2] * Wt[b][2];
+            out(16 + a, c.omgp2 * A.div3(24 + 3 * a) + c.gg * q);
         }
-        out(19, c.omgp2 * A.div3(33) + c.gp2 * gy * (p1 * pt2 - p2 * pt1 + p3 * pt4 - p4 * pt3));
+        out(19, c.omgp2 * A.div3(33) + c.ggy * (p1 * pt2 - p2 * pt1 + p3 * pt4 - p4 * pt3));
     }
 
     // ---- Higgs block: gradients, covariant derivatives, kt_phi (main_rk4.jl:337-407)
+    // Every rate below is one accumulator that each product term enters with
+    // a single fused multiply-add: the gauge terms of kt_phi are summed in
+    // units of g/2 and those of kt_W in units of g, the coupling applied once
+    // at the end.  The Higgs currents jW, jY are kept in units of g and g'.
     T ktp1, ktp2, ktp3, ktp4;
     T jW[3][3], jY[3];
     T cx = T(0), cy = T(0), cz = T(0), pdot = T(0);
@@ -127,39 +154,19 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         A.grad_lap(1, d2[0], d2[1], d2[2], l2);
         A.grad_lap(2, d3[0], d3[1], d3[2], l3);
         A.grad_lap(3, d4[0], d4[1], d4[2], l4);
-        const T Yv[3] = {Y2, Y3, Y4};
+        const T Yr[3] = {c.ryw * Y2, c.ryw * Y3, c.ryw * Y4};  // (g'/g) Y_i
         T D1[3], D2[3], D3[3], D4[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
-            cov_deriv(d1[i], d2[i], d3[i], d4[i], p1, p2, p3, p4, W[0][i], W[1][i], W[2][i], Yv[i], hgw, hgy, D1[i],
-                      D2[i], D3[i], D4[i]);
-        const T mag = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
-        const T pot = c.lam2 * (mag - c.vev2);
-        const T inv_mag = T(1) / mag;
-        // sum_i W_a_i * f_i
-#define WD(a, f) (W[a][0] * f[0] + W[a][1] * f[1] + W[a][2] * f[2])
-#define YD(f) (Y2 * f[0] + Y3 * f[1] + Y4 * f[2])
-        ktp1 = l1 + hgw * ((WD(0, d4) - WD(1, d3) + WD(2, d2)) + (WD(0, D4) - WD(1, D3) + WD(2, D2))) +
-               hgy * (YD(d2) + YD(D2)) - pot * p1 + T(0.5) * ((gw * G[2] + gy * S) * p2 - gw * G[1] * p3 + gw * G[0] * p4) -
-               c.hJex * p1 - c.gam * p1 * (p1 * pt1) * inv_mag;
-        ktp2 = l2 - hgw * ((WD(0, d3) + WD(1, d4) + WD(2, d1)) + (WD(0, D3) + WD(1, D4) + WD(2, D1))) -
-               hgy * (YD(d1) + YD(D1)) - pot * p2 - T(0.5) * ((gw * G[2] + gy * S) * p1 + gw * G[0] * p3 + gw * G[1] * p4) -
-               c.hJex * p2 - c.gam * p2 * (p2 * pt2) * inv_mag;
-        ktp3 = l3 + hgw * ((WD(0, d2) + WD(1, d1) - WD(2, d4)) + (WD(0, D2) + WD(1, D1) - WD(2, D4))) +
-               hgy * (YD(d4) + YD(D4)) - pot * p3 + T(0.5) * ((-gw * G[2] + gy * S) * p4 + gw * G[1] * p1 + gw * G[0] * p2) -
-               c.hJex * p3 - c.gam * p3 * (p3 * pt3) * inv_mag;
-        ktp4 = l4 - hgw * ((WD(0, d1) - WD(1, d2) - WD(2, d3)) + (WD(0, D1) - WD(1, D2) - WD(2, D3))) -
-               hgy * (YD(d3) + YD(D3)) - pot * p4 - T(0.5) * ((-gw * G[2] + gy * S) * p3 + gw * G[0] * p1 - gw * G[1] * p2) -
-               c.hJex * p4 - c.gam * p4 * (p4 * pt4) * inv_mag;
-#undef WD
-#undef YD
-        // Higgs currents of kt_W (main_rk4.jl:415,432,449,...) and kt_Y (:563)
+            cov_deriv_s(d1[i], d2[i], d3[i], d4[i], p1, p2, p3, p4, W[0][i], W[1][i], W[2][i], Yr[i], hgw, D1[i],
+                        D2[i], D3[i], D4[i]);
+        // Higgs currents of kt_W (main_rk4.jl:415,432,449,...) and kt_Y (:563), over g and g'
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            jW[0][i] = gw * (p1 * D4[i] - p2 * D3[i] + p3 * D2[i] - p4 * D1[i]);
-            jW[1][i] = gw * (-p1 * D3[i] - p2 * D4[i] + p3 * D1[i] + p4 * D2[i]);
-            jW[2][i] = gw * (p1 * D2[i] - p2 * D1[i] - p3 * D4[i] + p4 * D3[i]);
-            jY[i] = gy * (p1 * D2[i] - p2 * D1[i] + p3 * D4[i] - p4 * D3[i]);
+            jW[0][i] = p1 * D4[i] - p2 * D3[i] + p3 * D2[i] - p4 * D1[i];
+            jW[1][i] = -p1 * D3[i] - p2 * D4[i] + p3 * D1[i] + p4 * D2[i];
+            jW[2][i] = p1 * D2[i] - p2 * D1[i] - p3 * D4[i] + p4 * D3[i];
+            jY[i] = p1 * D2[i] - p2 * D1[i] + p3 * D4[i] - p4 * D3[i];
         }
         if constexpr (PART == 1) {
 #pragma unroll
@@ -175,17 +182,51 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
             cy = d1[1] * p1 + d2[1] * p2 + d3[1] * p3 + d4[1] * p4;
             cz = d1[2] * p1 + d2[2] * p2 + d3[2] * p3 + d4[2] * p4;
         }
+        // The gauge terms of kt_phi pair each gradient with its covariant
+        // derivative, (g/2) W.d phi + (g/2) W.D phi (main_rk4.jl:337-407), so
+        // they are taken once on the sums e = d + D (d is not needed after).
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            d1[i] += D1[i];
+            d2[i] += D2[i];
+            d3[i] += D3[i];
+            d4[i] += D4[i];
+        }
+        const T mag = p1 * p1 + p2 * p2 + p3 * p3 + p4 * p4;
+        // over g/2: the potential and external source 2 lambda (|Phi|^2 - v^2) + Jex/2,
+        // the damping gamma / |Phi|^2 (its 0/0 at |Phi| = 0 kept), the charges (g Gamma^3 +- g' Sigma)/2
+        const T potg = c.lam2h * (mag - c.vev2) + c.hJexh;
+        const T damp = c.gamh / mag;
+        const T q12 = G[2] + c.ryw * S, q34 = c.ryw * S - G[2];
+        T a1 = W[0][0] * d4[0] + W[0][1] * d4[1] + W[0][2] * d4[2] - W[1][0] * d3[0] - W[1][1] * d3[1] -
+               W[1][2] * d3[2] + W[2][0] * d2[0] + W[2][1] * d2[1] + W[2][2] * d2[2] + Yr[0] * d2[0] +
+               Yr[1] * d2[1] + Yr[2] * d2[2] + q12 * p2 - G[1] * p3 + G[0] * p4 - potg * p1 - damp * p1 * (p1 * pt1);
+        ktp1 = l1 + hgw * a1;
+        T a2 = -W[0][0] * d3[0] - W[0][1] * d3[1] - W[0][2] * d3[2] - W[1][0] * d4[0] - W[1][1] * d4[1] -
+               W[1][2] * d4[2] - W[2][0] * d1[0] - W[2][1] * d1[1] - W[2][2] * d1[2] - Yr[0] * d1[0] -
+               Yr[1] * d1[1] - Yr[2] * d1[2] - q12 * p1 - G[0] * p3 - G[1] * p4 - potg * p2 - damp * p2 * (p2 * pt2);
+        ktp2 = l2 + hgw * a2;
+        T a3 = W[0][0] * d2[0] + W[0][1] * d2[1] + W[0][2] * d2[2] + W[1][0] * d1[0] + W[1][1] * d1[1] +
+               W[1][2] * d1[2] - W[2][0] * d4[0] - W[2][1] * d4[1] - W[2][2] * d4[2] + Yr[0] * d4[0] +
+               Yr[1] * d4[1] + Yr[2] * d4[2] + q34 * p4 + G[1] * p1 + G[0] * p2 - potg * p3 - damp * p3 * (p3 * pt3);
+        ktp3 = l3 + hgw * a3;
+        T a4 = -W[0][0] * d1[0] - W[0][1] * d1[1] - W[0][2] * d1[2] + W[1][0] * d2[0] + W[1][1] * d2[1] +
+               W[1][2] * d2[2] + W[2][0] * d3[0] + W[2][1] * d3[1] + W[2][2] * d3[2] - Yr[0] * d3[0] -
+               Yr[1] * d3[1] - Yr[2] * d3[2] - q34 * p3 - G[0] * p1 + G[1] * p2 - potg * p4 - damp * p4 * (p4 * pt4);
+        ktp4 = l4 + hgw * a4;
     }
 
     // ---- SU(2) block, one colour at a time (field_strengths.jl:34-224)
+    //   kt W^a_i = lap W^a_i - d_i Gamma^a + g Q^a_i, Q accumulated over g
     T ktW[3][3];
     T F[3][3];  // F[b][0] = F^b_xy (W_b_23), [1] = F^b_xz (W_b_24), [2] = F^b_yz (W_b_34)
     if constexpr (kSU2) {
+    T Q[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
 #pragma unroll
-        for (int i = 0; i < 3; ++i) ktW[a][i] = jW[a][i] - gw * (W[b][i] * G[cc] - W[cc][i] * G[b]);
+        for (int i = 0; i < 3; ++i) Q[a][i] = jW[a][i] - W[b][i] * G[cc] + W[cc][i] * G[b];
     }
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
@@ -194,38 +235,38 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         for (int i = 0; i < 3; ++i) {
             T lap;
             A.grad_lap(4 + 3 * b + i, dW[i][0], dW[i][1], dW[i][2], lap);
-            ktW[b][i] += lap;
+            Q[b][i] = Q[b][i] + lap * c.igw;
         }
         const int b1 = (b + 1) % 3, b2 = (b + 2) % 3;
         F[b][0] = dW[1][0] - dW[0][1] + gw * (W[b1][0] * W[b2][1] - W[b1][1] * W[b2][0]);
         F[b][1] = dW[2][0] - dW[0][2] + gw * (W[b1][0] * W[b2][2] - W[b1][2] * W[b2][0]);
         F[b][2] = dW[2][1] - dW[1][2] + gw * (W[b1][1] * W[b2][2] - W[b1][2] * W[b2][1]);
-        // d_j W^b_i enters kt W^{b-1}_i with -g W^{b+1}_j and kt W^{b+1}_i with +g W^{b-1}_j
+        // d_j W^b_i enters Q^{b-1}_i with -W^{b+1}_j and Q^{b+1}_i with +W^{b-1}_j
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            ktW[b2][i] -= gw * (dW[i][0] * W[b1][0] + dW[i][1] * W[b1][1] + dW[i][2] * W[b1][2]);
-            ktW[b1][i] += gw * (dW[i][0] * W[b2][0] + dW[i][1] * W[b2][1] + dW[i][2] * W[b2][2]);
+            Q[b2][i] = Q[b2][i] - dW[i][0] * W[b1][0] - dW[i][1] * W[b1][1] - dW[i][2] * W[b1][2];
+            Q[b1][i] = Q[b1][i] + dW[i][0] * W[b2][0] + dW[i][1] * W[b2][1] + dW[i][2] * W[b2][2];
         }
     }
-    // -g sum_j (W^b_j F^c_ij - W^c_j F^b_ij) with F_ij antisymmetric
+    // -sum_j (W^b_j F^c_ij - W^c_j F^b_ij) with F_ij antisymmetric
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
         // i = x: j = y (F_xy), z (F_xz)
-        ktW[a][0] -= gw * ((W[b][1] * F[cc][0] - W[cc][1] * F[b][0]) + (W[b][2] * F[cc][1] - W[cc][2] * F[b][1]));
+        Q[a][0] = Q[a][0] - W[b][1] * F[cc][0] + W[cc][1] * F[b][0] - W[b][2] * F[cc][1] + W[cc][2] * F[b][1];
         // i = y: j = x (F_yx = -F_xy), z (F_yz)
-        ktW[a][1] -= gw * ((W[cc][0] * F[b][0] - W[b][0] * F[cc][0]) + (W[b][2] * F[cc][2] - W[cc][2] * F[b][2]));
+        Q[a][1] = Q[a][1] - W[cc][0] * F[b][0] + W[b][0] * F[cc][0] - W[b][2] * F[cc][2] + W[cc][2] * F[b][2];
         // i = z: j = x (F_zx = -F_xz), y (F_zy = -F_yz)
-        ktW[a][2] -= gw * ((W[cc][0] * F[b][1] - W[b][0] * F[cc][1]) + (W[cc][1] * F[b][2] - W[b][1] * F[cc][2]));
+        Q[a][2] = Q[a][2] - W[cc][0] * F[b][1] + W[b][0] * F[cc][1] - W[cc][1] * F[b][2] + W[b][1] * F[cc][2];
     }
-    // auxiliary gradient
+    // the coupling and the auxiliary gradient
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         T gx, gy_, gz;
         A.grad(16 + a, gx, gy_, gz);
-        ktW[a][0] -= gx;
-        ktW[a][1] -= gy_;
-        ktW[a][2] -= gz;
+        ktW[a][0] = gw * Q[a][0] - gx;
+        ktW[a][1] = gw * Q[a][1] - gy_;
+        ktW[a][2] = gw * Q[a][2] - gz;
     }
 
     }  // SU(2) block
@@ -241,9 +282,9 @@ __device__ __forceinline__ void site_rates(const Acc& A, const PhysCoef<T>& c, S
         FY[2] = dY[2][1] - dY[1][2];
         T gx, gy_, gz;
         A.grad(19, gx, gy_, gz);
-        ktY[0] = lap[0] + jY[0] - gx;
-        ktY[1] = lap[1] + jY[1] - gy_;
-        ktY[2] = lap[2] + jY[2] - gz;
+        ktY[0] = lap[0] + gy * jY[0] - gx;
+        ktY[1] = lap[1] + gy * jY[1] - gy_;
+        ktY[2] = lap[2] + gy * jY[2] - gz;
     }
 
     // ---- beta (CP-odd) terms

@@ -74,6 +74,7 @@ def _sig(L):
     L.ewpt_kc_bin_nums.argtypes = [C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_kc_bin_nums.restype = C.c_int64
     L.ewpt_diagnostics_noalloc.argtypes = [P, C.c_void_p, DP, C.c_void_p]
+    L.ewpt_fp64_peak.argtypes = [C.c_int32, DP, DP]
     E = C.c_void_p
     L.ewpt_ensemble_create.argtypes = [C.c_int32, C.POINTER(EwptParams), C.POINTER(E)]
     L.ewpt_ensemble_destroy.argtypes = [E]
@@ -125,6 +126,13 @@ def load():
         _sig(L)
         _lib = L
     return _lib
+
+
+def fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FLOP/s of the device (ewpt_fp64_peak)."""
+    f, t = C.c_double(), C.c_double()
+    check(load().ewpt_fp64_peak(int(device), C.byref(f), C.byref(t)))
+    return f.value
 
 
 def declared_symbols() -> list[str]:

@@ -275,6 +275,14 @@ int ewpt_mlp_gradients(ewpt_mlp* net, const float* x, const float* y, int32_t ba
 int ewpt_mlp_train_step(ewpt_mlp* net, const float* x, const float* y, int32_t batch, float lr, float weight_decay,
                         float* loss);
 
+/* Measured FP64 peak of `device` in FLOP/s (no counterpart in the
+ * reference): a kernel of independent fused multiply-add chains on every SM,
+ * timed with CUDA events (2 FLOPs per DFMA).  The denominator of the FP64
+ * stage kernels' compute roofline, which are bound by the FP64 pipe.
+ * *seconds (may be NULL) = the timed launch.  Synchronous; restores the
+ * caller's current device. */
+int ewpt_fp64_peak(int32_t device, double* flop_per_s, double* seconds);
+
 /* Snapshot diagnostics (the same 20 columns as ewpt_diagnostics) of a
  * caller-owned FP64 state, without allocating any device memory.  No
  * counterpart in the reference: it is for callers that cannot let the

@@ -351,6 +351,13 @@ int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pa
     return EWPT_OK;
 }
 
+int ewpt_set_wait_limit(ewpt_ctx* c, int64_t polls) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    c->wait_polls = polls < 0 ? -1 : polls;
+    ewpt_tma_set_spin(c);
+    return EWPT_OK;
+}
+
 int ewpt_get_tiling(const ewpt_ctx* c, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair) {
     if (!c || !bx || !by || !reg || !pair) return ewpt_fail(nullptr, EWPT_ERR_ARG, "NULL argument");
     *bx = c->tile.bx;

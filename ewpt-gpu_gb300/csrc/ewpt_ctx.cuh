@@ -24,6 +24,7 @@ struct ewpt_ctx {
     Fp32State y32{nullptr, nullptr};  // all five FP32 buffers: [36][lay.P]
     Layout lay{};
     void* tma = nullptr;  // TMA stage-kernel state (stage_tma.cu), made by the first TMA tiling
+    int64_t wait_polls = -1;  // limit of the TMA kernels' mbarrier waits in polls (< 0: default)
     Fp32Work w32{nullptr, nullptr, nullptr};
     // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
     double* scratch64 = nullptr;
@@ -65,6 +66,7 @@ void ewpt_release_aux(ewpt_ctx* c);
 bool tma_tiling_fits(const Grid& g, int by, int bz);
 int ewpt_tma_prepare(ewpt_ctx* c, int by, int bz);
 void ewpt_tma_release(ewpt_ctx* c);
+void ewpt_tma_set_spin(ewpt_ctx* c);
 int ewpt_tma_check(ewpt_ctx* c);
 cudaError_t launch_step_fp32_tma(ewpt_ctx* c, double Jex, double gam);
 // For the FP32 form, L is the hi/lo buffers' layout (ghost images of hi written).

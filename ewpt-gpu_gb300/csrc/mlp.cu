@@ -32,6 +32,7 @@ struct GemmArgs {
     float* C;
     int M, N, K, lda, ldb, ldc;
     int transA, transB;
+    long spin;  // polls before the commit wait gives up
 };
 
 __device__ __forceinline__ __nv_bfloat16 ldA(const GemmArgs& g, int m, int k) {
@@ -54,9 +55,14 @@ __device__ __forceinline__ __nv_bfloat16 ldB(const GemmArgs& g, int k, int n) {
 // gather), then one thread issues four tcgen05.mma (M 128, N 64, K 16) and
 // commits them to an mbarrier that every thread waits on before the slab is
 // overwritten.  Finally each warp reads its 32 TMEM lanes (rows) with
-// tcgen05.ld and writes C.  Every wait is bounded; a wait that runs out sets
-// g_tc_err and the kernel skips the remaining tensor-core work.
+// tcgen05.ld and writes C.  Every wait is bounded (g.spin polls, host-set
+// by ewpt_mlp_set_wait_limit, default kTcSpin).  A wait that runs out in any
+// thread ends the slab loop for the whole CTA (a block-wide vote, so every
+// thread leaves the loop at the same barrier), sets g_tc_err and skips the
+// remaining tensor-core work; before the TMEM columns are freed the CTA waits
+// again, with the full kTcSpin limit, for the MMAs already committed.
 constexpr int TC_M = 128, TC_N = 64, TC_K = 64;
+constexpr long kTcSpin = 1L << 22;
 __device__ int g_tc_err = 0;
 
 __device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -71,8 +77,8 @@ __host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
-    for (long it = 0; it < (1L << 22); ++it) {
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, long spin) {
+    for (long it = 0; it < spin; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -149,9 +155,13 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(ubar)
                          : "memory");
         }
-        if (!tc_wait(ubar, ks & 1)) {
+        const bool late = !tc_wait(ubar, ks & 1, g.spin);
+        if (__syncthreads_or(late)) {
+            // the MMAs of this slab still read shared memory and write TMEM:
+            // let them finish before the CTA leaves the loop
+            tc_wait(ubar, ks & 1, kTcSpin);
             ok = false;
-            atomicExch(&g_tc_err, 1);
+            if (tid == 0) atomicExch(&g_tc_err, 1);
         }
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -263,6 +273,7 @@ __global__ void k_sum_partials(const float* __restrict__ part, int n, float* out
 struct ewpt_mlp {
     int nin = 0, width = 0, nout = 0, maxb = 0, device = 0;
     cudaStream_t st = nullptr;
+    int64_t wait_polls = -1;  // limit of the GEMM's tensor-core waits in polls (< 0: default)
     int64_t np = 0;
     int64_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;
     float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
@@ -303,9 +314,10 @@ int mlp_cuda(ewpt_mlp* n, cudaError_t e, const char* what) {
     return mlp_fail(n, e == cudaErrorMemoryAllocation ? EWPT_ERR_OOM : EWPT_ERR_CUDA, s.c_str());
 }
 
-cudaError_t gemm(cudaStream_t st, const __nv_bfloat16* A, int lda, int transA, const __nv_bfloat16* B, int ldb,
+cudaError_t gemm(const ewpt_mlp* n, const __nv_bfloat16* A, int lda, int transA, const __nv_bfloat16* B, int ldb,
                  int transB, float* C, int ldc, int M, int N, int K) {
-    GemmArgs g{A, B, C, M, N, K, lda, ldb, ldc, transA, transB};
+    const cudaStream_t st = n->st;
+    GemmArgs g{A, B, C, M, N, K, lda, ldb, ldc, transA, transB, n->wait_polls < 0 ? kTcSpin : (long)n->wait_polls};
     const dim3 gr((N + TC_N - 1) / TC_N, (M + TC_M - 1) / TC_M);
     k_gemm_tc<<<gr, 128, 0, st>>>(g);
     return cudaGetLastError();
@@ -322,13 +334,13 @@ cudaError_t refresh_bf16(ewpt_mlp* n) {
 cudaError_t forward(ewpt_mlp* n, int B) {
     cudaError_t e;
     k_to_bf16<<<kEW, 256, 0, n->st>>>(n->xf, n->x0, (int64_t)B * n->nin);
-    e = gemm(n->st, n->x0, n->nin, 0, n->pb + n->oW1, n->nin, 1, n->z1, n->width, B, n->width, n->nin);
+    e = gemm(n, n->x0, n->nin, 0, n->pb + n->oW1, n->nin, 1, n->z1, n->width, B, n->width, n->nin);
     if (e) return e;
     k_bias_act<<<kEW, 256, 0, n->st>>>(n->z1, n->p + n->ob1, n->a1, B, n->width, 1);
-    e = gemm(n->st, n->a1, n->width, 0, n->pb + n->oW2, n->width, 1, n->z2, n->width, B, n->width, n->width);
+    e = gemm(n, n->a1, n->width, 0, n->pb + n->oW2, n->width, 1, n->z2, n->width, B, n->width, n->width);
     if (e) return e;
     k_bias_act<<<kEW, 256, 0, n->st>>>(n->z2, n->p + n->ob2, n->a2, B, n->width, 1);
-    e = gemm(n->st, n->a2, n->width, 0, n->pb + n->oW3, n->width, 1, n->z3, n->nout, B, n->nout, n->width);
+    e = gemm(n, n->a2, n->width, 0, n->pb + n->oW3, n->width, 1, n->z3, n->nout, B, n->nout, n->width);
     if (e) return e;
     k_bias_act<<<kEW, 256, 0, n->st>>>(n->z3, n->p + n->ob3, nullptr, B, n->nout, 0);
     return cudaGetLastError();
@@ -342,21 +354,21 @@ cudaError_t backward(ewpt_mlp* n, int B) {
     k_mse<<<nb, 256, 0, n->st>>>(n->z3, n->yf, n->dzf, n->dzb, (int64_t)B * O, 1.f / ((float)B * O), n->part);
     k_sum_partials<<<1, 1, 0, n->st>>>(n->part, nb, n->loss);
     // layer 3
-    e = gemm(n->st, n->dzb, O, 1, n->a2, W, 0, n->g + n->oW3, W, O, W, B);  // dW3 = dZ3^T A2
+    e = gemm(n, n->dzb, O, 1, n->a2, W, 0, n->g + n->oW3, W, O, W, B);  // dW3 = dZ3^T A2
     if (e) return e;
     k_colsum<<<(O + 127) / 128, 128, 0, n->st>>>(n->dzf, n->g + n->ob3, B, O);
-    e = gemm(n->st, n->dzb, O, 0, n->pb + n->oW3, W, 0, n->da, W, B, W, O);  // dA2 = dZ3 W3
+    e = gemm(n, n->dzb, O, 0, n->pb + n->oW3, W, 0, n->da, W, B, W, O);  // dA2 = dZ3 W3
     if (e) return e;
     k_gelu_bwd<<<kEW, 256, 0, n->st>>>(n->da, n->z2, n->dzf, n->dzb, (int64_t)B * W);
     // layer 2
-    e = gemm(n->st, n->dzb, W, 1, n->a1, W, 0, n->g + n->oW2, W, W, W, B);  // dW2 = dZ2^T A1
+    e = gemm(n, n->dzb, W, 1, n->a1, W, 0, n->g + n->oW2, W, W, W, B);  // dW2 = dZ2^T A1
     if (e) return e;
     k_colsum<<<(W + 127) / 128, 128, 0, n->st>>>(n->dzf, n->g + n->ob2, B, W);
-    e = gemm(n->st, n->dzb, W, 0, n->pb + n->oW2, W, 0, n->da, W, B, W, W);  // dA1 = dZ2 W2
+    e = gemm(n, n->dzb, W, 0, n->pb + n->oW2, W, 0, n->da, W, B, W, W);  // dA1 = dZ2 W2
     if (e) return e;
     k_gelu_bwd<<<kEW, 256, 0, n->st>>>(n->da, n->z1, n->dzf, n->dzb, (int64_t)B * W);
     // layer 1
-    e = gemm(n->st, n->dzb, W, 1, n->x0, I, 0, n->g + n->oW1, I, W, I, B);  // dW1 = dZ1^T X0
+    e = gemm(n, n->dzb, W, 1, n->x0, I, 0, n->g + n->oW1, I, W, I, B);  // dW1 = dZ1^T X0
     if (e) return e;
     k_colsum<<<(W + 127) / 128, 128, 0, n->st>>>(n->dzf, n->g + n->ob1, B, W);
     return cudaGetLastError();
@@ -445,6 +457,12 @@ int ewpt_mlp_destroy(ewpt_mlp* n) {
 const char* ewpt_mlp_last_error(const ewpt_mlp* n) { return n ? n->err.c_str() : ewpt_last_error(nullptr); }
 
 int64_t ewpt_mlp_num_params(const ewpt_mlp* n) { return n ? n->np : -1; }
+
+int ewpt_mlp_set_wait_limit(ewpt_mlp* n, int64_t polls) {
+    if (!n) return ewpt_fail(nullptr, EWPT_ERR_ARG, "net is NULL");
+    n->wait_polls = polls < 0 ? -1 : polls;
+    return EWPT_OK;
+}
 
 int ewpt_mlp_set_params(ewpt_mlp* n, const float* params) {
     if (!n || !params) return ewpt_fail(nullptr, EWPT_ERR_ARG, "NULL argument");

@@ -25,11 +25,15 @@
 // with thread 0 of the compute warps refilling the ring, the kernel ran at
 // half the speed.
 //
-// Every mbarrier wait is bounded.  A wait that runs out sets the context's
-// error word and stops the copies; the compute warps then run to the end
-// without further waits (results invalid, reported as EWPT_ERR_TIMEOUT by
-// the host), and the producer waits (bounded) for its last copies to land
-// before it exits.
+// Every mbarrier wait is bounded, by the context's wait limit (polls;
+// ewpt_set_wait_limit, default kSpin).  A compute thread whose wait runs out
+// sets the context's error word and runs to the end without further waits
+// or releases (results invalid, reported as EWPT_ERR_TIMEOUT by the host):
+// a warp releases a slot only after it saw that slot's copy land, so the
+// producer never issues a copy into a slot whose previous copy may still be
+// in flight.  A producer whose wait for a free slot runs out stops issuing;
+// it then waits for its last copies to land, always with the full kSpin
+// limit, before it exits, so no copy outlives the CTA.
 #include <cuda.h>
 
 #include <mutex>
@@ -191,8 +195,8 @@ __device__ __forceinline__ void mbar_arrive_nc(uint32_t bar, float dep) {
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar), "f"(dep));
 }
 // bounded wait for the phase of the given parity
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (long it = 0; it < kSpin; ++it)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long spin) {
+    for (long it = 0; it < spin; ++it)
         if (mbar_test(bar, parity)) return true;
     return false;
 }
@@ -214,6 +218,7 @@ struct Ring {
     const TmaMaps* maps;
     const EpiMaps* emaps;
     int* err;
+    long spin;               // polls before a wait gives up (the drain uses kSpin)
     int ntx, nty, ntiles;
     int x0, y0, z0;          // box origin (padded coordinates) of the current tile
     uint32_t tpar;           // parity offset of the current tile's boxes
@@ -261,7 +266,7 @@ struct Ring {
         if (ok) {
             got = 0;
             const uint32_t par = ((uint32_t)(j / NS) & 1u) ^ tpar;
-            for (long it = 0; it < kSpin && !got; ++it) got = mbar_test_nc(full(j % NS), par);
+            for (long it = 0; it < spin && !got; ++it) got = mbar_test_nc(full(j % NS), par);
             if (!got) {
                 ok = 0;
                 atomicExch(err, 1);
@@ -269,10 +274,11 @@ struct Ring {
         }
         return slots + (j % NS) * C::SLOT_FLOATS * 4 + opaque_zero(got);
     }
-    // this warp is done with box j (dep: a value computed from its reads)
+    // this warp is done with box j (dep: a value computed from its reads);
+    // after a wait of lane 0 ran out the warp releases nothing more
     __device__ __forceinline__ void release(int j, float dep) const {
         warp_sync_after(dep);
-        if ((threadIdx.x & 31) == 0) mbar_arrive_nc(empty(j % NS), dep);
+        if ((threadIdx.x & 31) == 0 && ok) mbar_arrive_nc(empty(j % NS), dep);
     }
     // producer warp, lane 0: every box of every tile of this CTA, each as soon
     // as the compute warps have released the previous occupant of its slot;
@@ -283,7 +289,7 @@ struct Ring {
             int ox, oy, oz;
             origin(t, ox, oy, oz);
             for (int j = 0; j < S::NLOAD; ++j, ++gq) {
-                if (gq >= NS && !mbar_wait(empty(j % NS), ((gq / NS) + 1) & 1)) {
+                if (gq >= NS && !mbar_wait(empty(j % NS), ((gq / NS) + 1) & 1, spin)) {
                     ok = 0;
                     atomicExch(err, 3);
                     break;
@@ -291,7 +297,7 @@ struct Ring {
                 issue(ox, oy, oz, j);
             }
         }
-        for (int q = gq - 1; q >= 0 && q >= gq - NS; --q) mbar_wait(full(q % NS), (q / NS) & 1);
+        for (int q = gq - 1; q >= 0 && q >= gq - NS; --q) mbar_wait(full(q % NS), (q / NS) & 1, kSpin);
     }
 };
 
@@ -465,7 +471,7 @@ template <int STAGE, bool BETA, int TBY, int TBZ>
 __global__ void __launch_bounds__(Cfg<TBY, TBZ>::NTHREADS, 1)
     k_stage_tma(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ TmaMaps M,
                 const __grid_constant__ EpiMaps E, const float* __restrict__ X, TmaBufs b,
-                float* __restrict__ xn, PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6, int* err) {
+                float* __restrict__ xn, PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6, int* err, long spin) {
     using C = Cfg<TBY, TBZ>;
     constexpr int NB = !kEpilogueInRing || STAGE == 1 ? 0 : STAGE == 4 ? 3 : 2;
     constexpr int BY = C::BY, BZ = C::BZ;
@@ -479,6 +485,7 @@ __global__ void __launch_bounds__(Cfg<TBY, TBZ>::NTHREADS, 1)
     R.maps = &M;
     R.emaps = &E;
     R.err = err;
+    R.spin = spin;
     R.ntx = g.nx / BX;
     R.nty = g.ny / BY;
     R.ntiles = R.ntx * R.nty * (g.nz / BZ);
@@ -563,6 +570,7 @@ struct TmaState {
     EpiMaps epi;  // [kacc, yhi, ylo]
     int* err = nullptr;
     int grid = 0;
+    long spin = kSpin;  // wait limit in polls (ewpt_set_wait_limit)
 };
 
 template <bool BETA, int TBY, int TBZ>
@@ -571,13 +579,13 @@ void step_tma(const Grid& g, const Layout& L, const TmaState& T, TmaBufs b, floa
     using C = Cfg<TBY, TBZ>;
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
     const int G = T.grid, n = C::NTHREADS, sm = C::SMEM_BYTES;
-    k_stage_tma<1, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.yhi, T.epi, b.yhi, b, xa, pc, sc, h2, w6, T.err);
+    k_stage_tma<1, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.yhi, T.epi, b.yhi, b, xa, pc, sc, h2, w6, T.err, T.spin);
     launch_ghost_fill(g, L, xa, st, true);
-    k_stage_tma<2, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, xb, pc, sc, h2, w6, T.err);
+    k_stage_tma<2, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, xb, pc, sc, h2, w6, T.err, T.spin);
     launch_ghost_fill(g, L, xb, st, true);
-    k_stage_tma<3, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xb, T.epi, xb, b, xa, pc, sc, h1, w6, T.err);
+    k_stage_tma<3, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xb, T.epi, xb, b, xa, pc, sc, h1, w6, T.err, T.spin);
     launch_ghost_fill(g, L, xa, st, true);
-    k_stage_tma<4, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, nullptr, pc, sc, z, w6, T.err);
+    k_stage_tma<4, BETA, TBY, TBZ><<<G, n, sm, st>>>(g, L, T.xa, T.epi, xa, b, nullptr, pc, sc, z, w6, T.err, T.spin);
     launch_ghost_fill(g, L, b.yhi, st, true);
 }
 
@@ -658,9 +666,17 @@ int ewpt_tma_prepare(ewpt_ctx* c, int by, int bz) {
     T->xa = m[1];
     T->xb = m[2];
     T->epi = em;
+    ewpt_tma_set_spin(c);
     const int ntiles = (c->g.nx / BX) * (c->g.ny / by) * (c->g.nz / bz);
     T->grid = std::min(ntiles, per_sm * nsm);
     return EWPT_OK;
+}
+
+// Wait limit of the TMA stage kernels' mbarrier waits, in polls (< 0: the
+// default kSpin); kept in the context and applied to its TMA state.
+void ewpt_tma_set_spin(ewpt_ctx* c) {
+    TmaState* T = static_cast<TmaState*>(c->tma);
+    if (T) T->spin = c->wait_polls < 0 ? kSpin : (long)c->wait_polls;
 }
 
 // Read and clear the error word of the TMA stage kernels (synchronous).

@@ -113,6 +113,8 @@ def _sig(L):
     L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     I32P = C.POINTER(C.c_int32)
     L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]
+    L.ewpt_set_wait_limit.argtypes = [V, C.c_int64]
+    L.ewpt_mlp_set_wait_limit.argtypes = [V, C.c_int64]
 
 
 def load():

@@ -99,6 +99,10 @@ class Lattice:
     def set_tiling(self, bx: int, by: int, reg: int = 0, pair: int = 0):
         self._chk(self.L.ewpt_set_tiling(self.h, int(bx), int(by), int(reg), int(pair)))
 
+    def set_wait_limit(self, polls: int):
+        """Limit of the TMA-staged kernels' device waits in polls (< 0: default)."""
+        self._chk(self.L.ewpt_set_wait_limit(self.h, int(polls)))
+
     def tiling(self) -> tuple:
         a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         self._chk(self.L.ewpt_get_tiling(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))

@@ -54,6 +54,10 @@ class MLP:
         except Exception:
             pass
 
+    def set_wait_limit(self, polls: int):
+        """Limit of the GEMM's tensor-core waits in polls (< 0: default)."""
+        self._chk(self.L.ewpt_mlp_set_wait_limit(self.h, int(polls)))
+
     @property
     def num_params(self) -> int:
         return int(self.L.ewpt_mlp_num_params(self.h))

@@ -120,6 +120,14 @@ int64_t ewpt_iteration(const ewpt_ctx* ctx);
  * lattice size and precision.  Default 32x4, 0, 0. */
 int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg, int32_t pair);
 int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair);
+/* Limit of the device-side waits of the TMA-staged stage kernels (pair = 2),
+ * in mbarrier polls; polls < 0 restores the default (2^22), 0 makes every
+ * wait give up at once.  A wait that runs out ends the kernel's copies
+ * safely, the step's results are invalid and the next ewpt_sync /
+ * ewpt_get_state returns EWPT_ERR_TIMEOUT; the context stays usable (set
+ * the state again).  For testing the bounded-wait path; no counterpart in
+ * the reference. */
+int ewpt_set_wait_limit(ewpt_ctx* ctx, int64_t polls);
 /* Wait for all work queued on the context. */
 int ewpt_sync(ewpt_ctx* ctx);
 /* The context's cudaStream_t, as an opaque pointer. */
@@ -264,6 +272,10 @@ int ewpt_mlp_create(int32_t n_in, int32_t width, int32_t n_out, int32_t max_batc
 int ewpt_mlp_destroy(ewpt_mlp* net);
 const char* ewpt_mlp_last_error(const ewpt_mlp* net);
 int64_t ewpt_mlp_num_params(const ewpt_mlp* net);
+/* Limit of the tensor-core waits of the MLP GEMM in mbarrier polls (< 0: the
+ * default 2^22; 0: every wait gives up at once, the call returns
+ * EWPT_ERR_TIMEOUT and the net stays usable).  For testing. */
+int ewpt_mlp_set_wait_limit(ewpt_mlp* net, int64_t polls);
 /* set (resets the optimizer state) / get the FP32 parameters */
 int ewpt_mlp_set_params(ewpt_mlp* net, const float* params);
 int ewpt_mlp_get_params(ewpt_mlp* net, float* params);

@@ -59,6 +59,10 @@ TRAFFIC_FP32 = 2804
 # an FMA as 2, and FP64 pipe instructions with single-use products fused.
 FLOPS_FP64 = 7300
 FP64_INST_EST = 4976
+# FP64 instructions per site-update the stage kernels execute (ncu
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum over the 4
+# launches at 80^3, per site): 3 x (454 + 126 + 604) + (454 + 126 + 568).
+FP64_INST_NCU = 4700
 N_BUBBLES = 64
 
 
@@ -295,8 +299,13 @@ def run_ours(args, ws, rank, local):
                              "flops_per_site_update": FLOPS_FP64,
                              "flops_source": "exact count of the kernels' per-site source (oracle/devphys.cu), "
                                              "FMA = 2 FLOPs",
-                             "fp64_inst_per_site_update_est": FP64_INST_EST,
-                             "pipe_frac_est": S * args.steps / t64 * FP64_INST_EST / (res["fp64"]["peak"] / 2),
+                             "pipe": {"fp64_inst_per_site_update": FP64_INST_NCU,
+                                      "source": "ncu DADD+DMUL+DFMA thread instructions at 80^3",
+                                      "achieved_ginst_s": S * args.steps / t64 * FP64_INST_NCU / 1e9,
+                                      "peak_ginst_s": res["fp64"]["peak"] / 2 / 1e9,
+                                      "frac": S * args.steps / t64 * FP64_INST_NCU / (res["fp64"]["peak"] / 2)},
+                             "note": "FLOP frac < 1 by construction: DADD and DMUL take a pipe slot for 1 FLOP; "
+                                     "the pipe frac is the FP64 instruction rate over the probe's",
                              "kernel": "k_stage_fp64 (4 launches/step)"},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,

@@ -59,10 +59,19 @@ struct ModeGeom {
     double kv[3];     // lattice momentum 2 sin(theta / 2) / dx
 };
 
-__device__ __forceinline__ ModeGeom mode_geom(const Grid& g, double dx, int64_t q) {
+// Mode q of the spectrum array: theta = 2 pi n / N per axis with n the FFT
+// index wrapped to [-N/2, N/2), or, with one_based, the reference's 1-based
+// array index (n = index + 1: the element bfft treats as frequency f gets
+// the amplitude of frequency f + 1, main_rk4.jl:5040-5046).
+__device__ __forceinline__ ModeGeom mode_geom(const Grid& g, double dx, int64_t q, bool one_based = false) {
     const int i = (int)(q % g.nx), j = (int)((q / g.nx) % g.ny), k = (int)(q / ((int64_t)g.nx * g.ny));
-    const int n[3] = {i < (g.nx + 1) / 2 ? i : i - g.nx, j < (g.ny + 1) / 2 ? j : j - g.ny,
-                      k < (g.nz + 1) / 2 ? k : k - g.nz};
+    int n[3] = {i < (g.nx + 1) / 2 ? i : i - g.nx, j < (g.ny + 1) / 2 ? j : j - g.ny,
+                k < (g.nz + 1) / 2 ? k : k - g.nz};
+    if (one_based) {
+        n[0] = i + 1;
+        n[1] = j + 1;
+        n[2] = k + 1;
+    }
     const int N[3] = {g.nx, g.ny, g.nz};
     ModeGeom m;
     m.k2 = 0.0;
@@ -120,6 +129,43 @@ __global__ void k_modes_transverse(Grid g, double dx, double T, double m, double
 #pragma unroll
         for (int d = 0; d < 3; ++d)
             out[d][q] = make_cuDoubleComplex(amp * (e1[d] * x[0] + e2[d] * x[1]), amp * (e1[d] * x[2] + e2[d] * x[3]));
+    }
+}
+
+// The same spectra from caller-supplied deviates, as the reference's own
+// kernels scale them (thermal_initializer_phi!, thermal_initializer_gauge!,
+// main_rk4.jl:5029-5152): one real deviate per Higgs mode; for a gauge field
+// the arrays r_1 r_2 r_3 (the polarisation draw), r_1_i r_2_i r_3_i (unused,
+// overwritten by the reference), x_1 x_2 x_3 x_4 at d[0..9] S apart.
+__global__ void k_dev_scalar(Grid g, double dx, double T, double m, double vol, int one_based,
+                             const double* __restrict__ d, cufftDoubleComplex* __restrict__ z) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < g.S; q += (int64_t)gridDim.x * blockDim.x) {
+        const ModeGeom mg = mode_geom(g, dx, q, one_based);
+        z[q] = make_cuDoubleComplex(amplitude(mg.k2, m, T, vol, false) * d[q], 0.0);
+    }
+}
+
+__global__ void k_dev_transverse(Grid g, double dx, double T, double m, double vol, int one_based,
+                                 const double* __restrict__ d, cufftDoubleComplex* __restrict__ z0,
+                                 cufftDoubleComplex* __restrict__ z1, cufftDoubleComplex* __restrict__ z2) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < g.S; q += (int64_t)gridDim.x * blockDim.x) {
+        const ModeGeom mg = mode_geom(g, dx, q, one_based);
+        const double* kv = mg.kv;
+        const double r[3] = {d[q], d[g.S + q], d[2 * g.S + q]};
+        const double x[4] = {d[6 * g.S + q], d[7 * g.S + q], d[8 * g.S + q], d[9 * g.S + q]};
+        double e1[3] = {r[1] * kv[2] - r[2] * kv[1], r[2] * kv[0] - r[0] * kv[2], r[0] * kv[1] - r[1] * kv[0]};
+        double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        n1 = n1 == 0.0 ? 1.0 : n1;
+        for (int c = 0; c < 3; ++c) e1[c] /= n1;
+        double e2[3] = {e1[1] * kv[2] - e1[2] * kv[1], e1[2] * kv[0] - e1[0] * kv[2], e1[0] * kv[1] - e1[1] * kv[0]};
+        double n2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
+        n2 = n2 == 0.0 ? 1.0 : n2;
+        for (int c = 0; c < 3; ++c) e2[c] /= n2;
+        const double amp = amplitude(mg.k2, m, T, vol, true);
+        cufftDoubleComplex* out[3] = {z0, z1, z2};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            out[c][q] = make_cuDoubleComplex(amp * (e1[c] * x[0] + e2[c] * x[1]), amp * (e1[c] * x[2] + e2[c] * x[3]));
     }
 }
 
@@ -250,6 +296,88 @@ extern "C" int ewpt_init_thermal(ewpt_ctx* c, double T, double mH, double mW, ui
     cudaError_t e = ewpt_commit_staged(c, dst);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     rc = ewpt_cuda_check(c, e, "init_thermal");
+    if (rc) return rc;
+    c->it = 0;
+    return EWPT_OK;
+}
+
+// Thermal IC from the caller's deviate arrays (the reference's construction,
+// main_rk4.jl:5348-5636, with its random draws supplied): dev holds 44
+// arrays of S doubles, host or device memory -- for W^1, W^2, W^3 and Y the
+// ten arrays r_1, r_2, r_3, r_1_i, r_2_i, r_3_i, x_1, x_2, x_3, x_4 in the
+// order run() draws them, then phi_1_k .. phi_4_k.  Gamma, Sigma and the
+// momenta are zero, as in run().
+extern "C" int ewpt_init_thermal_deviates(ewpt_ctx* c, double T, double mH, double mW, const double* dev,
+                                          int32_t on_device, int32_t flags) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!dev) return ewpt_fail(c, EWPT_ERR_ARG, "deviates is NULL");
+    if (flags & ~EWPT_THERMAL_ONE_BASED_MODES) return ewpt_fail(c, EWPT_ERR_ARG, "unknown thermal flags %d", flags);
+    int rc = ewpt_check_thermal(T, mH, mW);
+    if (rc) return ewpt_fail(c, rc, "%s", ewpt_last_error(nullptr));
+    if (c->view) return ewpt_fail(c, EWPT_ERR_STATE, "this context is a read-only view");
+    cudaSetDevice(c->p.device);
+    double* y;
+    rc = ewpt_staging64(c, &y, true);
+    if (rc) return rc;
+    const Grid& g = c->g;
+    const cudaStream_t st = c->st;
+    const double vol = (double)g.S * c->p.dx * c->p.dx * c->p.dx;
+    const int one_based = (flags & EWPT_THERMAL_ONE_BASED_MODES) ? 1 : 0;
+    cufftHandle plan;
+    if (cufftPlan3d(&plan, g.nz, g.ny, g.nx, CUFFT_Z2Z) != CUFFT_SUCCESS)
+        return ewpt_fail(c, EWPT_ERR_CUFFT, "cufftPlan3d (Z2Z) failed");
+    cufftSetStream(plan, st);
+    cufftDoubleComplex* z = nullptr;
+    double* d = nullptr;  // device copy of one group's deviates (host input)
+    cudaError_t e = cudaMemsetAsync(y, 0, (size_t)36 * g.S * 8, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&z, (size_t)3 * g.S * sizeof(cufftDoubleComplex), st);
+    if (e == cudaSuccess && !on_device) e = cudaMallocAsync(&d, (size_t)10 * g.S * 8, st);
+    bool fft_ok = true;
+    const int nb = 1216, nt = 256;
+    auto group = [&](int first, int n) -> const double* {
+        const double* src = dev + (size_t)first * g.S;
+        if (on_device || e != cudaSuccess) return src;
+        e = cudaMemcpyAsync(d, src, (size_t)n * g.S * 8, cudaMemcpyHostToDevice, st);
+        return d;
+    };
+    auto to_real = [&](cufftDoubleComplex* zc, int target) {
+        if (e != cudaSuccess || !fft_ok) return;
+        fft_ok = cufftExecZ2Z(plan, zc, zc, CUFFT_INVERSE) == CUFFT_SUCCESS;
+        if (fft_ok) k_real_part<<<nb, nt, 0, st>>>(g.S, zc, y + (size_t)target * g.S);
+        e = cudaGetLastError();
+    };
+    for (int gi = 0; gi < 4 && e == cudaSuccess && fft_ok; ++gi) {
+        const double* dd = group(10 * gi, 10);
+        if (e != cudaSuccess) break;
+        k_dev_transverse<<<nb, nt, 0, st>>>(g, c->p.dx, T, gi == 3 ? 0.0 : mW, vol, one_based, dd, z, z + g.S,
+                                            z + 2 * g.S);
+        e = cudaGetLastError();
+        const int base = gi == 3 ? 13 : 4 + 3 * gi;
+        for (int i = 0; i < 3; ++i) to_real(z + (size_t)i * g.S, base + i);
+    }
+    for (int a = 0; a < 4 && e == cudaSuccess && fft_ok; ++a) {
+        const double* dd = group(40 + a, 1);
+        if (e != cudaSuccess) break;
+        k_dev_scalar<<<nb, nt, 0, st>>>(g, c->p.dx, T, mH, vol, one_based, dd, z);
+        e = cudaGetLastError();
+        to_real(z, a);
+    }
+    if (z) {
+        const cudaError_t ef = cudaFreeAsync(z, st);
+        if (e == cudaSuccess) e = ef;
+    }
+    if (d) {
+        const cudaError_t ef = cudaFreeAsync(d, st);
+        if (e == cudaSuccess) e = ef;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cufftDestroy(plan);
+    if (!fft_ok) return ewpt_fail(c, EWPT_ERR_CUFFT, "cufftExecZ2Z failed");
+    rc = ewpt_cuda_check(c, e, "init_thermal_deviates");
+    if (rc) return rc;
+    e = ewpt_commit_staged(c, y);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    rc = ewpt_cuda_check(c, e, "init_thermal_deviates");
     if (rc) return rc;
     c->it = 0;
     return EWPT_OK;

@@ -22,6 +22,7 @@ FP64, FP32, DF64 = 0, 1, 2
 FIELD_B, FIELD_B2, FIELD_HIGGS, FIELD_DENSITY = 0, 1, 2, 3
 BUBBLE_REFERENCE, BUBBLE_TANH = 0, 1
 SPEC_LOG, SPEC_UNIQUE = 0, 1
+THERMAL_ONE_BASED_MODES = 1
 
 
 class EwptParams(C.Structure):
@@ -68,6 +69,8 @@ def _sig(L):
     L.ewpt_diagnostics.argtypes = [V, DP]
     L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
     L.ewpt_init_thermal.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_uint64]
+    L.ewpt_init_thermal_deviates.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_int32,
+                                             C.c_int32]
     L.ewpt_field_components.argtypes = [C.c_int32]
     L.ewpt_field_components.restype = C.c_int32
     L.ewpt_fields.argtypes = [V, C.c_int32, DP, C.c_int32]

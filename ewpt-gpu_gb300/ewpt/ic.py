@@ -273,6 +273,59 @@ def thermal(shape, dx, T=1.5, lam=0.129, gw=0.65, gy=0.35, vev=1.0, seed=0, mH=N
     return y
 
 
+def thermal_from_deviates(shape, dx, T, mH, mW, deviates, one_based=True) -> np.ndarray:
+    """The reference's thermal IC from given random draws (run()'s thermal
+    branch, main_rk4.jl:5348-5636, with thermal_initializer_gauge! and
+    thermal_initializer_phi!, :5029-5152); the host twin of
+    ewpt_init_thermal_deviates.  deviates: (44, S) in run()'s draw order --
+    for W^1, W^2, W^3, Y the arrays r_1, r_2, r_3, r_1_i, r_2_i, r_3_i, x_1..x_4,
+    then phi_1_k .. phi_4_k.  one_based: theta = 2 pi (index + 1) / N per axis
+    as the reference indexes its modes (else the FFT frequency).  Gamma,
+    Sigma and the momenta stay zero, as in run()."""
+    nx, ny, nz = shape
+    S = nx * ny * nz
+    dv = np.asarray(deviates, dtype=np.float64).reshape(44, nz, ny, nx)
+    idx = [np.arange(n) for n in (nz, ny, nx)]
+    if one_based:
+        th = [2.0 * math.pi * (i + 1) / n for i, n in zip(idx, (nz, ny, nx))]
+    else:
+        th = [2.0 * math.pi * np.where(i < (n + 1) // 2, i, i - n) / n for i, n in zip(idx, (nz, ny, nx))]
+    TZ, TY, TX = np.meshgrid(*th, indexing="ij")
+    k2 = 2.0 * ((1 - np.cos(TX)) + (1 - np.cos(TY)) + (1 - np.cos(TZ))) / dx ** 2
+    kv = [2.0 * np.sin(0.5 * t) / dx for t in (TX, TY, TZ)]
+    vol = S * dx ** 3
+
+    def amp(m, empty_k0):
+        w = np.sqrt(k2 + m * m)
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            a = np.where(w > 0, np.sqrt(1.0 / np.expm1(w / T) / (w * vol)), 0.0)
+        if empty_k0:
+            a = np.where(k2 == 0, 0.0, a)
+        return a
+
+    y = np.zeros((36, S))
+    for g in range(4):
+        d = dv[10 * g:10 * g + 10]
+        r, x = d[0:3], d[6:10]
+        e1 = [r[1] * kv[2] - r[2] * kv[1], r[2] * kv[0] - r[0] * kv[2], r[0] * kv[1] - r[1] * kv[0]]
+        n1 = np.sqrt(sum(c * c for c in e1))
+        n1[n1 == 0] = 1.0
+        e1 = [c / n1 for c in e1]
+        e2 = [e1[1] * kv[2] - e1[2] * kv[1], e1[2] * kv[0] - e1[0] * kv[2], e1[0] * kv[1] - e1[1] * kv[0]]
+        n2 = np.sqrt(sum(c * c for c in e2))
+        n2[n2 == 0] = 1.0
+        e2 = [c / n2 for c in e2]
+        a = amp(0.0 if g == 3 else mW, True)
+        base = 13 if g == 3 else 4 + 3 * g
+        for c in range(3):
+            z = a * (e1[c] * x[0] + e2[c] * x[1]) + 1j * a * (e1[c] * x[2] + e2[c] * x[3])
+            y[base + c] = np.real(_ifftn(z) * S).ravel()
+    aH = amp(mH, False)
+    for c in range(4):
+        y[c] = np.real(_ifftn(aH * dv[40 + c]) * S).ravel()
+    return y
+
+
 def gauss_charges(y, gw, gy):
     """SU(2) and U(1) charge densities of main_rk4.jl:603-655 (the terms
     multiplying gp2 in k_Gamma_a and k_Sigma)."""

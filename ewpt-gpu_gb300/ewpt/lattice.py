@@ -125,6 +125,19 @@ class Lattice:
         mW = p.gw * p.vev / 2.0 if mW is None else mW
         self._chk(self.L.ewpt_init_thermal(self.h, float(T), float(mH), float(mW), int(seed) & (2 ** 64 - 1)))
 
+    def init_thermal_deviates(self, T: float, deviates: np.ndarray, mH: float, mW: float = 0.0,
+                              one_based: bool = True):
+        """The reference's thermal IC from the caller's random draws
+        (ewpt_init_thermal_deviates): deviates (44, S) in run()'s draw order;
+        the reference itself uses mH = sqrt(meff_sq), mW = 0 and one-based
+        mode indices."""
+        d = np.ascontiguousarray(deviates, dtype=np.float64)
+        if d.shape != (44, self.S):
+            raise ValueError(f"deviates must be (44, {self.S})")
+        flags = _lib.THERMAL_ONE_BASED_MODES if one_based else 0
+        self._chk(self.L.ewpt_init_thermal_deviates(self.h, float(T), float(mH), float(mW),
+                                                    C.c_void_p(d.ctypes.data), 0, flags))
+
     # ------------------------------------------------------------ observables
     def diagnostics(self, allow_nonfinite: bool = False) -> np.ndarray:
         out = np.zeros(_lib.NDIAG)

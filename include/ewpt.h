@@ -219,6 +219,28 @@ int ewpt_init_bubbles(ewpt_ctx* ctx, int32_t nb, const double* bubbles, int32_t 
  * seed and the lattice.  Resets the iteration counter.  Synchronous. */
 int ewpt_init_thermal(ewpt_ctx* ctx, double T, double mH, double mW, uint64_t seed);
 
+enum ewpt_thermal_flags {
+    /* mode (i, j, k) of the spectrum array takes theta = 2 pi (index + 1) / N,
+     * the reference's 1-based indexing (main_rk4.jl:5040-5046), instead of the
+     * FFT frequency */
+    EWPT_THERMAL_ONE_BASED_MODES = 1
+};
+
+/* The reference's thermal IC from the caller's random draws (replaces the
+ * thermal branch of run(), main_rk4.jl:5348-5636, with its own deviate
+ * arrays): thermal_initializer_gauge! and thermal_initializer_phi!
+ * (:5029-5152) scale them and real(bfft(.)) makes the fields.  deviates
+ * holds 44 arrays of nx*ny*nz doubles (x fastest), host (on_device = 0) or
+ * device memory, in the order run() draws them: for W^1, W^2, W^3 and Y the
+ * ten arrays r_1, r_2, r_3, r_1_i, r_2_i, r_3_i, x_1, x_2, x_3, x_4, then
+ * phi_1_k .. phi_4_k.  Higgs w^2 = k^2 + mH^2 (the reference: mH^2 =
+ * meff_sq, parameters.jl:37), W^a w^2 = k^2 + mW^2 (the reference: mW = 0),
+ * Y massless; the gauge mode with k = 0 is left empty.  Gamma, Sigma and the
+ * momenta are zero, as in run().  flags: enum ewpt_thermal_flags.  Resets
+ * the iteration counter.  Synchronous. */
+int ewpt_init_thermal_deviates(ewpt_ctx* ctx, double T, double mH, double mW, const double* deviates,
+                               int32_t on_device, int32_t flags);
+
 /* ---------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which runs one
  * realization per process; each member here is an independent lattice with

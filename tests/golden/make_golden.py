@@ -2,7 +2,7 @@
 
 Run in a container where the reference checkout exists:
 
-    python tests/golden/make_golden.py [reference_root]
+    python tests/golden/make_golden.py <reference_root>
 
 The reference (Teerthal/EWPT-GPU) is Julia + CUDA.jl and Julia is not
 available, so this script mechanically translates the device-kernel bodies it
@@ -18,6 +18,8 @@ precision on seeded inputs:
   initializer!                   gpu-kernels-rk4/main_rk4.jl:4930-4946
   J_ext, damp                    gpu-kernels-rk4/main_rk4.jl:5154-5172
   K_c_mag, Kc_bin_nums, convolve_1d   gpu-kernels-rk4/spec_routines.jl:6-77
+  thermal_initializer_phi!, thermal_initializer_gauge!
+                                 gpu-kernels-rk4/main_rk4.jl:5029-5152
 
 The RK4 combination of the driver loop (main_rk4.jl:6182-6435) lives inside
 `run()` and is restated here as its four broadcast lines (mul, then add).
@@ -64,6 +66,13 @@ def load(ref: str) -> dict:
                       + ["Y_2_y", "Y_2_z", "Y_3_z"], ns)
     js.load_functions(os.path.join(base, "main_rk4.jl"),
                       ["rk4_step!", "initializer!", "J_ext", "damp"] + DENSITY_KERNELS, ns)
+    # the thermal kernels divide by exp(w/T) - 1 = 0 at the w = 0 mode before
+    # their branch discards it: IEEE division (inf, as in Julia), not Python's
+    nth = dict(js.RUNTIME, exp=lambda x: np.float64(math.exp(x)))
+    js.load_functions(os.path.join(base, "main_rk4.jl"), ["thermal_initializer_ϕ!", "thermal_initializer_gauge!"],
+                      nth)
+    ns["thermal_initializer_phi_b"] = nth["thermal_initializer_phi_b"]
+    ns["thermal_initializer_gauge_b"] = nth["thermal_initializer_gauge_b"]
     js.load_functions(os.path.join(base, "spec_routines.jl"),
                       ["K_c_mag", "Kc_bin_nums", "convolve_1d"], ns)
     ns["_sig"] = {n: js.signature(os.path.join(base, "main_rk4.jl"), n)
@@ -268,8 +277,68 @@ def bubble_case(ns):
                         its=its, jex=jex, damp=dmp)
 
 
+# deviate arrays of the thermal IC in the order run() draws them
+# (main_rk4.jl:5348-5636): for W^1, W^2, W^3 and Y the ten arrays r_1, r_2,
+# r_3, r_1_i, r_2_i, r_3_i, x_1, x_2, x_3, x_4, then phi_1_k .. phi_4_k
+THERMAL_GROUPS = [("W_1_2", "W_1_3", "W_1_4"), ("W_2_2", "W_2_3", "W_2_4"), ("W_3_2", "W_3_3", "W_3_4"),
+                  ("Y_2", "Y_3", "Y_4")]
+
+
+def thermal_case(ns, seed=2718):
+    """The reference's thermal IC on fixed deviates: each gauge group's
+    arrays go through thermal_initializer_gauge! (r_1..r_3 become the real
+    and r_1_i..r_3_i the imaginary part of the spectrum) and then
+    real(bfft(re + i im)); the Higgs deviates through thermal_initializer_phi!
+    and real(bfft(.)) (main_rk4.jl:5348-5636).  bfft is the unnormalised
+    backward transform: numpy's ifftn times the number of sites.  Gamma,
+    Sigma and the momenta stay zero, as in run()."""
+    shape = (8, 7, 10)
+    nx, ny, nz = shape
+    S = nx * ny * nz
+    rng = np.random.default_rng(seed)
+    dev = rng.normal(0.0, math.sqrt(2.0), size=(44, S))
+    gw, gy, gp2, vev, dx, T = 0.65, 0.35, 0.99, 1.0, 0.25, 1.5
+    meff_sq = 8119.43 / 174.0 ** 2  # parameters.jl:37
+    fields = np.zeros((36, S))
+    spec = np.zeros((16, S), dtype=complex)
+
+    def bfft(z):
+        return np.fft.ifftn(z.reshape(shape, order="F")) * S
+
+    np.seterr(divide="ignore")
+    for g, names in enumerate(THERMAL_GROUPS):
+        d = dev[10 * g:10 * g + 10].copy()
+        arr = [as_jarr(d[q], shape) for q in range(10)]
+        r1, r2, r3, r1i, r2i, r3i, x1, x2, x3, x4 = arr
+        fn = ns["thermal_initializer_gauge_b"]
+        for k in range(1, nz + 1):
+            for j in range(1, ny + 1):
+                for i in range(1, nx + 1):
+                    fn(gw, gy, gp2, vev, dx, T, nx, ny, nz, r1, r2, r3, r1i, r2i, r3i, x1, x2, x3, x4, i, j, k)
+        base = 4 + 3 * g
+        for c in range(3):
+            z = d[c] + 1j * d[3 + c]
+            spec[base + c] = z
+            fields[base + c] = bfft(z).real.ravel(order="F")
+    d = dev[40:44].copy()
+    arr = [as_jarr(d[q], shape) for q in range(4)]
+    fn = ns["thermal_initializer_phi_b"]
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                fn(*arr, gw, gy, gp2, vev, dx, T, meff_sq, nx, ny, nz, i, j, k)
+    for a in range(4):
+        spec[a] = d[a]
+        fields[a] = bfft(d[a]).real.ravel(order="F")
+    np.savez_compressed(os.path.join(HERE, "ref_thermal.npz"), shape=np.array(shape), deviates=dev, fields=fields,
+                        spec=spec, T=T, meff_sq=meff_sq, dx=dx)
+    print("thermal max |field|", np.abs(fields).max(axis=1)[:16])
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference_root>")
+    ref = sys.argv[1]
     ns = load(ref)
     # the damp() fixture needs the driver's gamma_inp global
     ns["γ_inp"] = 0.3
@@ -283,6 +352,7 @@ def main():
     case(ns, "b", (7, 8, 9), pb, dt=0.05, Jex=0.0, gam=0.0, seed=99)
     spectrum_case(ns)
     bubble_case(ns)
+    thermal_case(ns)
     orders_case(ref, ns)
 
 

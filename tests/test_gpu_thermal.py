@@ -149,3 +149,27 @@ def test_thermal_ic_uses_the_context_stencil():
     g_norm = math.sqrt((y[16:19] ** 2).sum() * p.dx ** 3)
     s_norm = math.sqrt((y[19] ** 2).sum() * p.dx ** 3)
     assert d[18] < 1e-12 * g_norm and d[19] < 1e-12 * s_norm
+
+
+@pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32, ewpt.DF64])
+def test_device_thermal_from_deviates_matches_reference_kernels(golden_dir, prec):
+    """ewpt_init_thermal_deviates with the reference's conventions (1-based
+    mode indices, massless gauge modes, mH^2 = meff_sq) against the
+    reference's own thermal_initializer_gauge!/phi! + bfft evaluated on the
+    same deviates (tests/golden/ref_thermal.npz): every field to 1e-12 of its
+    largest value (cuFFT against numpy's FFT); Gamma, Sigma and the momenta
+    zero, as in run()."""
+    import math
+    import os
+
+    g = dict(np.load(os.path.join(golden_dir, "ref_thermal.npz")))
+    shape = tuple(int(v) for v in g["shape"])
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=float(g["dx"]), dt=0.025, precision=prec)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(np.ones((36, p.sites)))  # overwritten everywhere
+        lat.init_thermal_deviates(float(g["T"]), g["deviates"], mH=math.sqrt(float(g["meff_sq"])), mW=0.0)
+        y = lat.get_state()
+    ref = g["fields"]
+    scale = np.abs(ref[:16]).max(axis=1, keepdims=True)
+    assert (np.abs(y[:16] - ref[:16]) / scale).max() < 1e-12
+    assert np.abs(y[16:]).max() == 0.0

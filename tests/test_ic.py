@@ -62,3 +62,26 @@ def test_bubbles_reference_profile_matches_oracle():
     for b in range(3):
         orc.bubble_rmag(op, yo, coords[pick[b]], ewpt.ic.gen_phi(*hoft[b], signs[b]), p.mH)
     np.testing.assert_allclose(y[:4], yo[:4], rtol=1e-13, atol=1e-15)
+
+
+def test_thermal_from_deviates_matches_reference_kernels(golden_dir):
+    """The host twin of ewpt_init_thermal_deviates against the reference's
+    thermal_initializer_gauge!/phi! + bfft run on the same deviates
+    (tests/golden/ref_thermal.npz, made by make_golden.py from the
+    reference's source): with the reference's 1-based mode indices, massless
+    gauge modes and mH^2 = meff_sq, every field agrees to 1e-12."""
+    import math
+    import os
+
+    g = dict(np.load(os.path.join(golden_dir, "ref_thermal.npz")))
+    shape = tuple(int(v) for v in g["shape"])
+    y = ewpt.ic.thermal_from_deviates(shape, float(g["dx"]), float(g["T"]), math.sqrt(float(g["meff_sq"])), 0.0,
+                                 g["deviates"], one_based=True)
+    ref = g["fields"]
+    scale = np.abs(ref[:16]).max(axis=1, keepdims=True)
+    assert (np.abs(y[:16] - ref[:16]) / scale).max() < 1e-12
+    assert not y[16:].any() and not ref[16:].any()
+    # with FFT-frequency modes the spectrum moves by one mode per axis: not the reference's
+    y0 = ewpt.ic.thermal_from_deviates(shape, float(g["dx"]), float(g["T"]), math.sqrt(float(g["meff_sq"])), 0.0,
+                                  g["deviates"], one_based=False)
+    assert (np.abs(y0[:16] - ref[:16]) / scale).max() > 1e-3

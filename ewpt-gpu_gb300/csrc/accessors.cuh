@@ -94,12 +94,22 @@ struct SiteAcc {
                s.a3 * (ld(a + 2, oz[2]) - ld(a + 2, oz[5]));
     }
 
-    // site (i, j, k) of an nx x ny x nz box
-    __device__ __forceinline__ void place(int i, int j, int k, int nx, int ny, int nz) {
-        c = i + nx * (j + ny * k);
+    // site (i, j, k) of an nx x ny x nz box; with zg > 0 interior plane k of
+    // a z-slab whose zg ghost planes on each side hold the neighbours' planes
+    __device__ __forceinline__ void place(int i, int j, int k, int nx, int ny, int nz, int zg = 0) {
         axis_offsets(i, nx, 1, ox);
         axis_offsets(j, ny, nx, oy);
-        axis_offsets(k, nz, nx * ny, oz);
+        if (zg == 0) {
+            c = i + nx * (j + ny * k);
+            axis_offsets(k, nz, nx * ny, oz);
+        } else {
+            c = i + nx * (j + ny * (k + zg));
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                oz[d] = (d + 1) * nx * ny;
+                oz[d + 3] = -(d + 1) * nx * ny;
+            }
+        }
     }
     // site (i, j, k) of a ghosted layout: y and z neighbours are plain
     // strides (ghost cells), x neighbours wrap (the x ghost cells are kept

@@ -194,6 +194,7 @@ int ewpt_destroy(ewpt_ctx* c) {
 // Device buffer holding the packed FP64 state (for FP32 contexts, a staging
 // buffer that split/join convert through).
 int ewpt_staging64(ewpt_ctx* c, double** out, bool in) {
+    if (c->slab) return ewpt_fail(c, EWPT_ERR_STATE, "slab contexts take packed states (ewpt_set_state_packed)");
     if (c->p.precision == EWPT_FP64 || (in && c->p.precision == EWPT_DF64)) {
         *out = c->y;  // DF64: converted in place after the upload
         return EWPT_OK;
@@ -226,6 +227,7 @@ static cudaError_t copy_runs(double* dev, const double* const* arrays, int64_t S
 
 int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t on_device) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (c->slab) return ewpt_fail(c, EWPT_ERR_STATE, "slab contexts take packed states (ewpt_set_state_packed)");
     if (!arrays) return ewpt_fail(c, EWPT_ERR_ARG, "arrays is NULL");
     for (int a = 0; a < 36; ++a)
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
@@ -247,6 +249,7 @@ cudaError_t ewpt_commit_staged(ewpt_ctx* c, const double* staged) {
 
 int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_device) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (c->slab) return ewpt_fail(c, EWPT_ERR_STATE, "slab contexts give packed states (ewpt_get_state_packed)");
     if (!arrays) return ewpt_fail(c, EWPT_ERR_ARG, "arrays is NULL");
     for (int a = 0; a < 36; ++a)
         if (!arrays[a]) return ewpt_fail(c, EWPT_ERR_ARG, "arrays[%d] is NULL", a);
@@ -266,6 +269,13 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
 int ewpt_set_state_packed(ewpt_ctx* c, const double* buf, int32_t on_device) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     if (!buf) return ewpt_fail(c, EWPT_ERR_ARG, "buf is NULL");
+    if (c->slab) {
+        cudaSetDevice(c->p.device);
+        cudaError_t e = ewpt_slab_copy(c, const_cast<double*>(buf), true, on_device);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        c->it = 0;
+        return ewpt_cuda_check(c, e, "slab set_state");
+    }
     const double* a[36];
     for (int q = 0; q < 36; ++q) a[q] = buf + (size_t)q * c->g.S;
     return ewpt_set_state(c, a, on_device);
@@ -274,6 +284,12 @@ int ewpt_set_state_packed(ewpt_ctx* c, const double* buf, int32_t on_device) {
 int ewpt_get_state_packed(ewpt_ctx* c, double* buf, int32_t on_device) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     if (!buf) return ewpt_fail(c, EWPT_ERR_ARG, "buf is NULL");
+    if (c->slab) {
+        cudaSetDevice(c->p.device);
+        cudaError_t e = ewpt_slab_copy(c, buf, false, on_device);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        return ewpt_cuda_check(c, e, "slab get_state");
+    }
     double* a[36];
     for (int q = 0; q < 36; ++q) a[q] = buf + (size_t)q * c->g.S;
     return ewpt_get_state(c, a, on_device);
@@ -290,6 +306,7 @@ static double damp_of(const ewpt_params& p, int64_t it) {
 static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double gam) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
     if (c->view) return ewpt_fail(c, EWPT_ERR_STATE, "this context is a read-only view");
+    if (c->slab) return ewpt_fail(c, EWPT_ERR_STATE, "a slab steps stage by stage between ghost exchanges");
     if (nsteps < 0) return ewpt_fail(c, EWPT_ERR_ARG, "nsteps < 0");
     if (expl && (!std::isfinite(Jex) || !std::isfinite(gam)))
         return ewpt_fail(c, EWPT_ERR_ARG, "non-finite Jex/gamma");

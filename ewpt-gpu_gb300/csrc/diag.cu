@@ -352,6 +352,8 @@ int ewpt_ensure_scratch64(ewpt_ctx* c) {
 }
 
 int ewpt_state64(ewpt_ctx* c, const double** out) {
+    if (c->slab)
+        return ewpt_fail(c, EWPT_ERR_STATE, "a slab holds part of a lattice: gather the state (ewpt_slabs_get_state)");
     if (c->p.precision == EWPT_FP64) {
         *out = c->y;
         return EWPT_OK;

@@ -11,6 +11,10 @@ struct ewpt_ctx {
     cudaStream_t st = nullptr;
     int64_t it = 0;  // RK4 iterations done (the reference's loop counter)
     bool view = false;  // state buffer only (an ensemble member's FP64 view): no stepping
+    // z-slab of a larger lattice (slab.cu): g.nz interior planes starting at
+    // global plane z0 of nz_global, g.zg ghost planes per z face
+    bool slab = false;
+    int z0 = 0, nz_global = 0;
     Tiling tile = kDefaultTiling;  // stage-kernel launch shape
     // FP64 form: state y, accumulator yn, stage inputs xa/xb, each [36][S]
     double* y = nullptr;
@@ -55,6 +59,8 @@ int ewpt_ensure_scratch64(ewpt_ctx* c);
 // context's form (FP32 split with ghost faces, DF64 pairs), on c->st.
 extern "C" int ewpt_staging64(ewpt_ctx* c, double** out, bool in);
 extern "C" cudaError_t ewpt_commit_staged(ewpt_ctx* c, const double* staged);
+// Interior of a slab context <-> a packed [36][nx ny nz] buffer (slab.cu).
+cudaError_t ewpt_slab_copy(ewpt_ctx* c, double* packed, bool to_dev, int32_t on_device);
 // Thermal IC (thermal.cu) into an FP64 [36][S] device state y, synchronous
 // on st; ewpt_check_thermal validates T and the masses.
 int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, double mW, uint64_t seed,

@@ -9,10 +9,14 @@
 #define EWPT_NFIELD 20  // phi(4) W(9) Y(3) Gamma(3) Sigma(1)
 #define EWPT_NMOM 16    // momenta of phi, W, Y
 
-// Lattice geometry of one periodic box.
+// Lattice geometry of one periodic box, or of one z-slab of it: with zg > 0
+// the arrays hold zg ghost planes below and above the nz interior planes
+// (S = nx*ny*(nz + 2 zg) is then the array stride) and the FP64 stage
+// kernels read z neighbours from the ghost planes instead of wrapping.
 struct Grid {
     int nx, ny, nz;
-    int64_t S;  // nx*ny*nz
+    int64_t S;  // nx*ny*nz, or the padded array stride of a slab
+    int zg = 0;
 };
 
 // Storage of one FP32-form [36][.] array set: element (i, j, k) of array a
@@ -159,6 +163,9 @@ int tiling_max_threads(int reg);
 
 cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+// One stage (1..4) of that step (z-slabs exchange ghost planes between stages).
+cudaError_t launch_stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa,
+                              double* xb, const ewpt_params& p, double Jex, double gam, cudaStream_t st);
 // FP64 stage and rates with the alternative stencil orders (stage_orders.cu)
 cudaError_t launch_step_fp64_order(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                                    const ewpt_params& p, double Jex, double gam, cudaStream_t st);

@@ -46,7 +46,7 @@ __device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return false;
-    A.place(i, j, k, g.nx, g.ny, g.nz);
+    A.place(i, j, k, g.nx, g.ny, g.nz, g.zg);
     A.s = sc;
     return true;
 }
@@ -269,6 +269,40 @@ static void step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, dou
     k_stage_fp64<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.);
     k_stage_fp64<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 3., dt);
     k_stage_fp64<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
+}
+
+template <bool BETA, int REG>
+static void stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa, double* xb,
+                       const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+    const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
+    switch (stage) {
+        case 1: k_stage_fp64<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack(y, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 6., dt / 2.); break;
+        case 2: k_stage_fp64<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.); break;
+        case 3: k_stage_fp64<3, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xb, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 3., dt); break;
+        default: k_stage_fp64<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
+    }
+}
+
+template <bool BETA>
+static void stage_fp64_r(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa, double* xb,
+                         const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+    if (t.reg == 1)
+        stage_fp64<BETA, 1>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+    else if (t.reg == 2)
+        stage_fp64<BETA, 2>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+    else
+        stage_fp64<BETA, 0>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+}
+
+cudaError_t launch_stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa,
+                              double* xb, const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+    const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
+    const StencilCoef<double> sc = make_stencil<double>(p.dx);
+    if (p.beta_w != 0.0 || p.beta_y != 0.0)
+        stage_fp64_r<true>(g, t, stage, y, yn, xa, xb, pc, sc, p.dt, st);
+    else
+        stage_fp64_r<false>(g, t, stage, y, yn, xa, xb, pc, sc, p.dt, st);
+    return cudaGetLastError();
 }
 
 template <bool BETA>

@@ -10,6 +10,7 @@ from ._lib import DF64, FP32, FP64, EwptError, load
 from .ensemble import Ensemble
 from .lattice import DIAG_NAMES, Lattice, kc_bin_nums, rk4_rates_device
 from .params import Params, baseline_couplings
+from .slabs import DistributedSlab, SlabGroup
 
-__all__ = ["Ensemble", "Lattice", "Params", "baseline_couplings", "ic", "FP32", "FP64", "DF64", "EwptError", "load",
+__all__ = ["Ensemble", "Lattice", "Params", "SlabGroup", "DistributedSlab", "baseline_couplings", "ic", "FP32", "FP64", "DF64", "EwptError", "load",
            "DIAG_NAMES", "kc_bin_nums", "rk4_rates_device", "_lib"]

@@ -117,6 +117,25 @@ def _sig(L):
     I32P = C.POINTER(C.c_int32)
     L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]
     L.ewpt_set_wait_limit.argtypes = [V, C.c_int64]
+    I32A = C.POINTER(C.c_int32)
+    L.ewpt_slabs_create.argtypes = [P, C.c_int32, I32A, I32A, C.POINTER(V)]
+    L.ewpt_slabs_destroy.argtypes = [V]
+    L.ewpt_slabs_last_error.argtypes = [V]
+    L.ewpt_slabs_last_error.restype = C.c_char_p
+    L.ewpt_slabs_count.argtypes = [V]
+    L.ewpt_slabs_count.restype = C.c_int32
+    L.ewpt_slabs_set_state.argtypes = [V, C.c_void_p, C.c_int32]
+    L.ewpt_slabs_get_state.argtypes = [V, C.c_void_p, C.c_int32]
+    L.ewpt_slabs_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_slabs_step.argtypes = [V, C.c_int32]
+    L.ewpt_slabs_step_explicit.argtypes = [V, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_slabs_sync.argtypes = [V]
+    L.ewpt_slabs_stream.argtypes = [V, C.c_int32]
+    L.ewpt_slabs_stream.restype = C.c_void_p
+    L.ewpt_create_slab.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(V)]
+    L.ewpt_slab_pack.argtypes = [V, C.c_int32, C.c_void_p, C.c_void_p]
+    L.ewpt_slab_unpack.argtypes = [V, C.c_int32, C.c_void_p, C.c_void_p]
+    L.ewpt_slab_stage.argtypes = [V, C.c_int32, C.c_double, C.c_double]
     L.ewpt_mlp_set_wait_limit.argtypes = [V, C.c_int64]
 
 

@@ -242,6 +242,55 @@ int ewpt_init_thermal_deviates(ewpt_ctx* ctx, double T, double mH, double mW, co
                                int32_t on_device, int32_t flags);
 
 /* ---------------------------------------------------------------------
+ * z-slab decomposition (replaces the MPI decomposition of
+ * gpu-kernels-rk4/main_rk4_multiple.jl: update_halo! and boundary_x/y/z,
+ * :69-212, host-staged MPI.Sendrecv! of 3-plane ghost layers after every
+ * stage).  An nx x ny x nz lattice is cut along z into slabs; a slab keeps 3
+ * ghost planes below and above its interior, filled from the neighbouring
+ * slabs (periodic in z) before each RK4 stage.  FP64 form, 6th-order
+ * stencils; a decomposed step gives the same bits as ewpt_step on the whole
+ * lattice.
+ *
+ * One process, any number of slabs on one or several GPUs: */
+typedef struct ewpt_slabs ewpt_slabs;
+/* n slabs of nz_local[m] planes (NULL: an even split, the first nz % n
+ * slabs one plane more; each >= 3), slab m on devices[m] (NULL: p->device).
+ * p describes the whole lattice.  State starts at zero. */
+int ewpt_slabs_create(const ewpt_params* p, int32_t n, const int32_t* nz_local, const int32_t* devices,
+                      ewpt_slabs** out);
+int ewpt_slabs_destroy(ewpt_slabs* slabs);
+const char* ewpt_slabs_last_error(const ewpt_slabs* slabs);
+int32_t ewpt_slabs_count(const ewpt_slabs* slabs);
+/* the whole lattice's packed [36][nx*ny*nz] state, host or device memory
+ * (set resets the iteration counter); synchronous */
+int ewpt_slabs_set_state(ewpt_slabs* slabs, const double* packed, int32_t on_device);
+int ewpt_slabs_get_state(ewpt_slabs* slabs, double* packed, int32_t on_device);
+/* launch shape of every slab's stage kernels (ewpt_set_tiling, pair = 0) */
+int ewpt_slabs_set_tiling(ewpt_slabs* slabs, int32_t bx, int32_t by, int32_t reg);
+/* nsteps RK4 steps (the J_ext/damp schedule of ewpt_step, or explicit
+ * values), asynchronous on the slabs' streams */
+int ewpt_slabs_step(ewpt_slabs* slabs, int32_t nsteps);
+int ewpt_slabs_step_explicit(ewpt_slabs* slabs, int32_t nsteps, double Jex, double gamma);
+int ewpt_slabs_sync(ewpt_slabs* slabs);
+void* ewpt_slabs_stream(ewpt_slabs* slabs, int32_t m);
+
+/* One slab per process (a rank per GPU); the caller moves the packed faces.
+ * A slab context of planes [z0, z0 + nz_local) of the lattice p (FP64,
+ * 6th order, nz_local >= 3); its state I/O is ewpt_set/get_state_packed on
+ * the packed [36][nx*ny*nz_local] interior.  One step is, for stage = 1..4:
+ *   ewpt_slab_pack(ctx, stage, lo, hi)        the bottom / top 3 interior
+ *       planes of the stage's input into lo / hi ([36][3*nx*ny] doubles each,
+ *       device memory); send lo to the slab below, hi to the slab above;
+ *   ewpt_slab_unpack(ctx, stage, below, above) the planes received from the
+ *       slab below (its hi) and above (its lo) into the ghost planes;
+ *   ewpt_slab_stage(ctx, stage, Jex, gamma)   the stage kernel.
+ * All three are asynchronous on the context's stream (ewpt_stream). */
+int ewpt_create_slab(const ewpt_params* p, int32_t z0, int32_t nz_local, ewpt_ctx** out);
+int ewpt_slab_pack(ewpt_ctx* ctx, int32_t stage, double* lo, double* hi);
+int ewpt_slab_unpack(ewpt_ctx* ctx, int32_t stage, const double* below, const double* above);
+int ewpt_slab_stage(ewpt_ctx* ctx, int32_t stage, double Jex, double gamma);
+
+/* ---------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which runs one
  * realization per process; each member here is an independent lattice with
  * its own size, couplings and dt, in the FP32 form).  One RK4 stage over all

@@ -19,6 +19,13 @@ electric fields (each one removes about half of the remaining
 constraint residual; 20 leave ~1e-7 of the charge density).  `--forms`
 picks the forms; fp64 always runs, as the reference.
 
+`--control EPS` adds the control run "fp64_perturbed": the FP64 form from
+the same initial state with every value multiplied by (1 + EPS xi), xi
+standard normal (seeded), reported against FP64 like the other forms.  It
+measures how far the dynamics alone carries a perturbation of the size of
+FP32 rounding (EPS ~ 1e-7): a bar on the FP32 form tighter than this
+control's difference cannot be met by any arithmetic.
+
 Reported per form: the total energy every `every` steps and its drift
 |E(t) - E(0)| / |E(0)|, the Gauss-constraint violation ||G_W|| and ||G_Y||
 (diagnostic columns 14 and 16) and, against FP64, the largest relative field
@@ -39,9 +46,10 @@ from .lattice import Lattice
 from .params import baseline_couplings
 
 
-def evolve(p, y0, steps, every, tune=True):
+def evolve(p, y0, steps, every, tune=True, perturb=0.0, perturb_seed=11):
     """y0: the (36, S) initial state, or ("device", T, seed) for the device
-    thermal IC (identical in every form up to the form's storage)."""
+    thermal IC (identical in every form up to the form's storage).
+    perturb: relative size of the seeded perturbation of the initial state."""
     hist, t0 = [], time.perf_counter()
     # the sweep runs on its own scratch lattice: pick the shape before this one exists
     tile = autotune.best_tiling(p) if tune else None
@@ -50,6 +58,13 @@ def evolve(p, y0, steps, every, tune=True):
             lat.init_thermal(y0[1], seed=y0[2])
         else:
             lat.set_state(y0)
+        if perturb:
+            y = lat.get_state()
+            rng = np.random.default_rng(perturb_seed)
+            for q in range(y.shape[0]):
+                y[q] *= 1.0 + perturb * rng.standard_normal(y.shape[1])
+            lat.set_state(y)
+            del y
         if tile:
             lat.set_tiling(*tile)
         d = lat.diagnostics(allow_nonfinite=True)
@@ -76,15 +91,17 @@ FORMS = {"fp64": _lib.FP64, "fp32": _lib.FP32, "df64": _lib.DF64}
 
 
 def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df64"), gauss_iters=20,
-           device_ic=False):
+           device_ic=False, control=0.0):
     shape = (N, N, N)
     t0 = time.perf_counter()
     y0 = ("device", T, seed) if device_ic else ic.thermal(shape, 0.25, T=T, seed=seed, gauss_iters=gauss_iters)
     t_ic = time.perf_counter() - t0
     runs = {}
-    for name in ["fp64"] + [f for f in forms if f != "fp64"]:
-        p = baseline_couplings(N=N, dx=0.25, dt=0.025, precision=FORMS[name])
-        r = evolve(p, y0, steps, every)
+    names = ["fp64"] + [f for f in forms if f != "fp64"] + (["fp64_perturbed"] if control else [])
+    for name in names:
+        prec = FORMS["fp64" if name == "fp64_perturbed" else name]
+        p = baseline_couplings(N=N, dx=0.25, dt=0.025, precision=prec)
+        r = evolve(p, y0, steps, every, perturb=control if name == "fp64_perturbed" else 0.0)
         if name != "fp64":  # keep one end state besides the reference's (16 GB each at 384^3)
             r["field_err"] = rel_field_err(r.pop("y"), runs["fp64"]["y"])
         runs[name] = r
@@ -93,7 +110,7 @@ def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df
     smask = ref["spec"] > 1e-12 * ref["spec"].max()
     out = dict(lattice=list(shape), steps=steps, every=every, T=T, seed=seed, dt=0.025, dx=0.25,
                ic="device (momenta zero)" if device_ic else f"host (Gauss projection, {gauss_iters} iterations)",
-               ic_seconds=t_ic, forms={})
+               ic_seconds=t_ic, control_perturbation=control, forms={})
     for name, r in runs.items():
         h = r["hist"]
         f = dict(seconds=r["seconds"], tile=r["tile"],
@@ -121,13 +138,15 @@ def main(argv=None):
     ap.add_argument("--gauss-iters", type=int, default=20)
     ap.add_argument("--device-ic", action="store_true",
                     help="the device thermal IC (ewpt_init_thermal: the reference's construction, momenta zero)")
+    ap.add_argument("--control", type=float, default=0.0,
+                    help="relative size of the perturbed-IC FP64 control run (0: none)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     forms = [f for f in a.forms.split(",") if f]
     bad = [f for f in forms if f not in FORMS]
     if bad:
         ap.error(f"unknown forms {bad}; choose from {sorted(FORMS)}")
-    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters, a.device_ic)
+    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters, a.device_ic, a.control)
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:

@@ -453,7 +453,7 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* e, int32_t m, int32_t nb, const double*
     return EWPT_OK;
 }
 
-int ewpt_ensemble_init_thermal(ewpt_ens* e, int32_t m, double T, double mH, double mW, uint64_t seed) {
+static int ens_thermal(ewpt_ens* e, int32_t m, double T, double mH, double mW, uint64_t seed, int gauss_iters) {
     int rc = ens_member_check(e, m);
     if (rc) return rc;
     rc = ewpt_check_thermal(T, mH, mW);
@@ -463,13 +463,24 @@ int ewpt_ensemble_init_thermal(ewpt_ens* e, int32_t m, double T, double mH, doub
     rc = ens_view(e, m, &v);
     if (rc) return rc;
     std::string err;
-    rc = ewpt_thermal_fill(v->g, v->p, T, mH, mW, seed, v->y, v->st, &err);  // after the view's join (same stream)
+    // after the view's join (same stream)
+    rc = ewpt_thermal_fill(v->g, v->p, T, mH, mW, seed, v->y, v->st, &err, gauss_iters);
     if (rc) return ens_fail(e, rc, ("init_thermal: " + err).c_str());
     const EnsMember& M = e->tab[m];
     cudaError_t ce =
         launch_fp32_split(v->g, plain_layout(v->g), v->y, Fp32State{e->b.yhi + M.off, e->b.ylo + M.off}, e->st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
     return ens_cuda(e, ce, "ensemble init_thermal");
+}
+
+int ewpt_ensemble_init_thermal(ewpt_ens* e, int32_t m, double T, double mH, double mW, uint64_t seed) {
+    return ens_thermal(e, m, T, mH, mW, seed, -1);
+}
+
+int ewpt_ensemble_init_thermal_gauss(ewpt_ens* e, int32_t m, double T, double mH, double mW, uint64_t seed,
+                                     int32_t gauss_iters) {
+    if (gauss_iters < 0) return ens_fail(e, EWPT_ERR_ARG, "gauss_iters < 0");
+    return ens_thermal(e, m, T, mH, mW, seed, gauss_iters);
 }
 
 int ewpt_ensemble_diagnostics(ewpt_ens* e, int32_t m, double out[EWPT_NDIAG]) {

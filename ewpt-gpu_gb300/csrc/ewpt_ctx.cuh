@@ -64,7 +64,7 @@ cudaError_t ewpt_slab_copy(ewpt_ctx* c, double* packed, bool to_dev, int32_t on_
 // Thermal IC (thermal.cu) into an FP64 [36][S] device state y, synchronous
 // on st; ewpt_check_thermal validates T and the masses.
 int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, double mW, uint64_t seed,
-                      double* y, cudaStream_t st, std::string* err);
+                      double* y, cudaStream_t st, std::string* err, int gauss_iters);
 int ewpt_check_thermal(double T, double mH, double mW);
 void ewpt_release_aux(ewpt_ctx* c);
 // Bubble IC kernel (init.cu) on an FP64 state (y) or an FP32 hi/lo state.

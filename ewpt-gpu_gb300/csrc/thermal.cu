@@ -86,18 +86,21 @@ __device__ __forceinline__ ModeGeom mode_geom(const Grid& g, double dx, int64_t 
 
 __device__ __forceinline__ double occupation(double w, double T) { return w > 0.0 ? 1.0 / expm1(w / T) : 0.0; }
 
-// amp(k) = sqrt(n(w) / (w V)), w^2 = k^2 + m^2; zero at k = 0 when massless_k0.
-__device__ __forceinline__ double amplitude(double k2, double m, double T, double vol, bool empty_k0) {
+// amp(k) = sqrt(n(w) / (w V)) for a field, sqrt(n(w) w / V) for its momentum
+// (mom), w^2 = k^2 + m^2; zero at k = 0 when empty_k0.
+__device__ __forceinline__ double amplitude(double k2, double m, double T, double vol, bool empty_k0,
+                                            bool mom = false) {
     if (empty_k0 && k2 == 0.0) return 0.0;
     const double w = sqrt(k2 + m * m);
-    return w > 0.0 ? sqrt(occupation(w, T) / (w * vol)) : 0.0;
+    if (!(w > 0.0)) return 0.0;
+    return mom ? sqrt(occupation(w, T) * w / vol) : sqrt(occupation(w, T) / (w * vol));
 }
 
 __global__ void k_modes_scalar(Grid g, double dx, double T, double m, double vol, uint64_t key, int stream,
-                               cufftDoubleComplex* __restrict__ z) {
+                               cufftDoubleComplex* __restrict__ z, int mom) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < g.S; q += (int64_t)gridDim.x * blockDim.x) {
         const ModeGeom mg = mode_geom(g, dx, q);
-        const double amp = amplitude(mg.k2, m, T, vol, false);
+        const double amp = amplitude(mg.k2, m, T, vol, false, mom != 0);
         double a, b;
         normal_pair(key, stream, q, a, b);
         z[q] = make_cuDoubleComplex(amp * a, amp * b);
@@ -106,7 +109,7 @@ __global__ void k_modes_scalar(Grid g, double dx, double T, double m, double vol
 
 __global__ void k_modes_transverse(Grid g, double dx, double T, double m, double vol, uint64_t key, int stream,
                                    cufftDoubleComplex* __restrict__ z0, cufftDoubleComplex* __restrict__ z1,
-                                   cufftDoubleComplex* __restrict__ z2) {
+                                   cufftDoubleComplex* __restrict__ z2, int mom) {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < g.S; q += (int64_t)gridDim.x * blockDim.x) {
         const ModeGeom mg = mode_geom(g, dx, q);
         const double* kv = mg.kv;
@@ -123,7 +126,7 @@ __global__ void k_modes_transverse(Grid g, double dx, double T, double m, double
         double n2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
         n2 = n2 == 0.0 ? 1.0 : n2;
         for (int d = 0; d < 3; ++d) e2[d] /= n2;
-        const double amp = amplitude(mg.k2, m, T, vol, true);
+        const double amp = amplitude(mg.k2, m, T, vol, true, mom != 0);
         // x1 + i x3 on e1, x2 + i x4 on e2 (thermal_initializer_gauge!)
         cufftDoubleComplex* out[3] = {z0, z1, z2};
 #pragma unroll
@@ -216,9 +219,15 @@ cudaError_t divergence(const Grid& g, int order, double dx, const double* f, int
 
 }  // namespace
 
+int ewpt_gauss_project_fp64(const Grid& g, const ewpt_params& p, double* y, int iters, cudaStream_t st,
+                            std::string* err);
+
 // Fill an FP64 [36][S] state with the thermal IC (device pointers, stream st).
+// gauss_iters < 0: momenta zero (the reference); >= 0: thermal momenta as
+// well (amplitude sqrt(n w / V), Higgs streams 4-7, gauge 24 + 4 c), then
+// that many iterations of the Gauss projection (gauss.cu).
 int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, double mW, uint64_t seed,
-                      double* y, cudaStream_t st, std::string* err) {
+                      double* y, cudaStream_t st, std::string* err, int gauss_iters) {
     const double vol = (double)g.S * p.dx * p.dx * p.dx;
     cufftHandle plan;
     if (cufftPlan3d(&plan, g.nz, g.ny, g.nx, CUFFT_Z2Z) != CUFFT_SUCCESS) {
@@ -240,19 +249,32 @@ int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, 
         e = cudaGetLastError();
     };
     // Higgs phi_1..4: streams 0..3
+    const bool mom = gauss_iters >= 0;
     for (int a = 0; a < 4 && e == cudaSuccess; ++a) {
-        k_modes_scalar<<<nb, nt, 0, st>>>(g, p.dx, T, mH, vol, key, a, z);
+        k_modes_scalar<<<nb, nt, 0, st>>>(g, p.dx, T, mH, vol, key, a, z, 0);
         e = cudaGetLastError();
         to_real(z, a);
+        if (mom && e == cudaSuccess && fft_ok) {
+            k_modes_scalar<<<nb, nt, 0, st>>>(g, p.dx, T, mH, vol, key, 4 + a, z, 1);
+            e = cudaGetLastError();
+            to_real(z, 20 + a);
+        }
     }
-    // W^a (arrays 4 + 3a + i), streams 8 + 4a .. ; Y (13 + i), streams 24 ..
+    // W^a (arrays 4 + 3a + i), streams 8 + 4a .. ; Y (13 + i), streams 20 ..;
+    // their momenta (24 + 3a + i, 33 + i) streams 24 + 4 c
     for (int c = 0; c < 4 && e == cudaSuccess && fft_ok; ++c) {
         const bool is_y = c == 3;
         k_modes_transverse<<<nb, nt, 0, st>>>(g, p.dx, T, is_y ? 0.0 : mW, vol, key, 8 + 4 * c, z, z + g.S,
-                                              z + 2 * g.S);
+                                              z + 2 * g.S, 0);
         e = cudaGetLastError();
         const int base = is_y ? 13 : 4 + 3 * c;
         for (int i = 0; i < 3; ++i) to_real(z + (size_t)i * g.S, base + i);
+        if (mom && e == cudaSuccess && fft_ok) {
+            k_modes_transverse<<<nb, nt, 0, st>>>(g, p.dx, T, is_y ? 0.0 : mW, vol, key, 24 + 4 * c, z, z + g.S,
+                                                  z + 2 * g.S, 1);
+            e = cudaGetLastError();
+            for (int i = 0; i < 3; ++i) to_real(z + (size_t)i * g.S, 20 + base + i);
+        }
     }
     // Gamma^a = div W^a (arrays 16..18), Sigma = div Y (19)
     if (e == cudaSuccess && fft_ok) e = divergence(g, p.stencil_order, p.dx, y + (size_t)4 * g.S, 3, y + (size_t)16 * g.S, st);
@@ -271,6 +293,7 @@ int ewpt_thermal_fill(const Grid& g, const ewpt_params& p, double T, double mH, 
         *err = cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? EWPT_ERR_OOM : EWPT_ERR_CUDA;
     }
+    if (gauss_iters > 0) return ewpt_gauss_project_fp64(g, p, y, gauss_iters, st, err);
     return EWPT_OK;
 }
 
@@ -291,7 +314,7 @@ extern "C" int ewpt_init_thermal(ewpt_ctx* c, double T, double mH, double mW, ui
     rc = ewpt_staging64(c, &dst, true);
     if (rc) return rc;
     std::string err;
-    rc = ewpt_thermal_fill(c->g, c->p, T, mH, mW, seed, dst, c->st, &err);
+    rc = ewpt_thermal_fill(c->g, c->p, T, mH, mW, seed, dst, c->st, &err, -1);
     if (rc) return ewpt_fail(c, rc, "init_thermal: %s", err.c_str());
     cudaError_t e = ewpt_commit_staged(c, dst);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -378,6 +401,32 @@ extern "C" int ewpt_init_thermal_deviates(ewpt_ctx* c, double T, double mH, doub
     e = ewpt_commit_staged(c, y);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     rc = ewpt_cuda_check(c, e, "init_thermal_deviates");
+    if (rc) return rc;
+    c->it = 0;
+    return EWPT_OK;
+}
+
+// The thermal IC with thermal momenta projected onto the Gauss law (the
+// benchmark's precision configuration: "momenta set by the Gauss-constraint
+// projection"); gauss_iters iterations of gauss.cu's projection.
+extern "C" int ewpt_init_thermal_gauss(ewpt_ctx* c, double T, double mH, double mW, uint64_t seed,
+                                       int32_t gauss_iters) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    int rc = ewpt_check_thermal(T, mH, mW);
+    if (rc) return ewpt_fail(c, rc, "%s", ewpt_last_error(nullptr));
+    if (gauss_iters < 0) return ewpt_fail(c, EWPT_ERR_ARG, "gauss_iters < 0");
+    if (c->view) return ewpt_fail(c, EWPT_ERR_STATE, "this context is a read-only view");
+    if (c->p.stencil_order != 6) return ewpt_fail(c, EWPT_ERR_ARG, "the projection uses the 6th-order stencil");
+    cudaSetDevice(c->p.device);
+    double* dst;
+    rc = ewpt_staging64(c, &dst, true);
+    if (rc) return rc;
+    std::string err;
+    rc = ewpt_thermal_fill(c->g, c->p, T, mH, mW, seed, dst, c->st, &err, gauss_iters);
+    if (rc) return ewpt_fail(c, rc, "init_thermal_gauss: %s", err.c_str());
+    cudaError_t e = ewpt_commit_staged(c, dst);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    rc = ewpt_cuda_check(c, e, "init_thermal_gauss");
     if (rc) return rc;
     c->it = 0;
     return EWPT_OK;

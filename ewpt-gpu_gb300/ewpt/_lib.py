@@ -69,6 +69,10 @@ def _sig(L):
     L.ewpt_diagnostics.argtypes = [V, DP]
     L.ewpt_spectrum.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, DP, DP, DP, DP, C.POINTER(C.c_int32)]
     L.ewpt_init_thermal.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_uint64]
+    L.ewpt_init_thermal_gauss.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int32]
+    L.ewpt_gauss_project.argtypes = [V, C.c_int32]
+    L.ewpt_ensemble_init_thermal_gauss.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                                   C.c_uint64, C.c_int32]
     L.ewpt_init_thermal_deviates.argtypes = [V, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_int32,
                                              C.c_int32]
     L.ewpt_field_components.argtypes = [C.c_int32]

@@ -81,6 +81,16 @@ class Ensemble:
         self._chk(self.L.ewpt_ensemble_init_thermal(self.h, m, float(T), float(mH), float(mW),
                                                     int(seed) & (2 ** 64 - 1)))
 
+    def init_thermal_gauss(self, m: int, T: float, seed: int = 0, gauss_iters: int = 20, mH: float | None = None,
+                           mW: float | None = None):
+        """Member m from the thermal IC with Gauss-projected thermal momenta
+        (ewpt_ensemble_init_thermal_gauss)."""
+        p = self.members[m]
+        mH = math.sqrt(2.0 * p.lam) * p.vev if mH is None else mH
+        mW = p.gw * p.vev / 2.0 if mW is None else mW
+        self._chk(self.L.ewpt_ensemble_init_thermal_gauss(self.h, m, float(T), float(mH), float(mW),
+                                                          int(seed) & (2 ** 64 - 1), int(gauss_iters)))
+
     def set_drive(self, m: int, Jex: float, gamma: float):
         self._chk(self.L.ewpt_ensemble_set_drive(self.h, m, float(Jex), float(gamma)))
 

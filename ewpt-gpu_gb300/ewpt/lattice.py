@@ -125,6 +125,20 @@ class Lattice:
         mW = p.gw * p.vev / 2.0 if mW is None else mW
         self._chk(self.L.ewpt_init_thermal(self.h, float(T), float(mH), float(mW), int(seed) & (2 ** 64 - 1)))
 
+    def init_thermal_gauss(self, T: float, seed: int = 0, gauss_iters: int = 20, mH: float | None = None,
+                           mW: float | None = None):
+        """ewpt_init_thermal_gauss: the thermal IC with thermal momenta
+        projected onto the Gauss law (gauss_iters iterations)."""
+        p = self.params
+        mH = math.sqrt(2.0 * p.lam) * p.vev if mH is None else mH
+        mW = p.gw * p.vev / 2.0 if mW is None else mW
+        self._chk(self.L.ewpt_init_thermal_gauss(self.h, float(T), float(mH), float(mW), int(seed) & (2 ** 64 - 1),
+                                                 int(gauss_iters)))
+
+    def gauss_project(self, iters: int = 20):
+        """ewpt_gauss_project: project the state's electric fields onto the Gauss law."""
+        self._chk(self.L.ewpt_gauss_project(self.h, int(iters)))
+
     def init_thermal_deviates(self, T: float, deviates: np.ndarray, mH: float, mW: float = 0.0,
                               one_based: bool = True):
         """The reference's thermal IC from the caller's random draws

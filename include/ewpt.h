@@ -219,6 +219,25 @@ int ewpt_init_bubbles(ewpt_ctx* ctx, int32_t nb, const double* bubbles, int32_t 
  * seed and the lattice.  Resets the iteration counter.  Synchronous. */
 int ewpt_init_thermal(ewpt_ctx* ctx, double T, double mH, double mW, uint64_t seed);
 
+/* The benchmark's precision-configuration IC: ewpt_init_thermal's fields
+ * with thermal momenta as well (Higgs and gauge, amplitude sqrt(n(w) w / V),
+ * the gauge momenta transverse, zero at k = 0), then gauss_iters iterations
+ * of ewpt_gauss_project.  No counterpart in the reference, whose thermal
+ * momenta are zero.  Resets the iteration counter.  Synchronous. */
+int ewpt_init_thermal_gauss(ewpt_ctx* ctx, double T, double mH, double mW, uint64_t seed, int32_t gauss_iters);
+
+/* Projects the current state's electric fields onto the discrete Gauss law
+ * of the evolution (the gp2 parts of k_Gamma, k_Sigma, main_rk4.jl:603-655):
+ * d_i E^a_i = rho^a, d_i E^Y_i = rho_Y with the 6th-order central difference.
+ * Each of `iters` iterations first moves the Higgs momenta along the charge
+ * generators so that the charges have no component in the zero and
+ * staggered modes the divergence cannot produce, then subtracts grad chi
+ * from each group's E, chi from a Fourier-space solve; the SU(2) charge
+ * depends on E, so the residual falls by iterations.  The fields, Gamma and
+ * Sigma are unchanged.  Any form (FP32/DF64 states are projected in FP64).
+ * No counterpart in the reference.  Synchronous. */
+int ewpt_gauss_project(ewpt_ctx* ctx, int32_t iters);
+
 enum ewpt_thermal_flags {
     /* mode (i, j, k) of the spectrum array takes theta = 2 pi (index + 1) / N,
      * the reference's 1-based indexing (main_rk4.jl:5040-5046), instead of the
@@ -315,6 +334,9 @@ int ewpt_ensemble_init_bubbles(ewpt_ens* ens, int32_t m, int32_t nb, const doubl
 /* ewpt_init_thermal for member m (the same state as a single context of
  * the member's parameters and the same seed, split into the FP32 form) */
 int ewpt_ensemble_init_thermal(ewpt_ens* ens, int32_t m, double T, double mH, double mW, uint64_t seed);
+/* ewpt_init_thermal_gauss for member m */
+int ewpt_ensemble_init_thermal_gauss(ewpt_ens* ens, int32_t m, double T, double mH, double mW, uint64_t seed,
+                                     int32_t gauss_iters);
 /* constant Jex and gamma of member m for the following steps */
 int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
 /* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent

@@ -340,10 +340,15 @@ def test_fp32_tma_tiles_reject_bad_contexts():
         assert lat.tiling() == (32, 4, 0, 0)
 
 
-def test_fp32_form_tracks_fp64():
-    """FP32 form vs FP64 on a smooth bubble IC: fields within 1e-4 of FP64
-    after 100 steps, energy drift and Gauss violation within 2x of FP64
-    (plus a floor at FP32 round-off of the total energy), B spectrum 1e-4."""
+@pytest.mark.parametrize("ic_kind", ["bubbles", "thermal"])
+def test_fp32_form_tracks_fp64(ic_kind):
+    """The FP32 form's bars against FP64 after 100 steps, with no floors:
+    fields within 1e-4 (per array, of its largest value), the energy change
+    |E(t) - E(0)| and the Gauss violation ||G_W||, ||G_Y|| within 2x of
+    FP64's, and the B spectrum within 1e-4 per shell.  Both ICs move the
+    FP64 energy measurably (about 2.4e-3 E0 for the bubbles and 0.13 E0 for
+    the T = 1.5 thermal state over 100 steps, the constraint formulation's
+    own drift), so each 2x bar can fail."""
     shape = (32, 32, 32)
     p64 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025)
     p32 = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=ewpt.FP32)
@@ -351,7 +356,10 @@ def test_fp32_form_tracks_fp64():
     res = {}
     for name, p in (("64", p64), ("32", p32), ("32x2", p32), ("32tma", p32)):
         with ewpt.Lattice(p) as lat:
-            lat.set_state(y0)
+            if ic_kind == "thermal":
+                lat.init_thermal(1.5, seed=3)
+            else:
+                lat.set_state(y0)
             if name == "32x2":
                 lat.set_tiling(32, 4, 0, 1)
             if name == "32tma":
@@ -362,15 +370,15 @@ def test_fp32_form_tracks_fp64():
     y64 = res["64"][0]
     e0 = res["64"][1][13]
     drift64 = abs(res["64"][2][13] - e0)
-    g64 = res["64"][2][14]
+    assert drift64 > 1e-3 * abs(e0)  # the bar has something to measure
+    gw64, gy64 = res["64"][2][14], res["64"][2][16]
     s64 = res["64"][3]["mean"]
     m = s64 > 1e-12 * s64.max()
     for name in ("32", "32x2", "32tma"):
         y32 = res[name][0]
         assert rel_err(y32[:20], y64[:20]) < 1e-4
-        drift32 = abs(res[name][2][13] - e0)
-        assert drift32 <= 2.0 * drift64 + 1e-6 * abs(e0)
-        assert res[name][2][14] <= 2.0 * g64 + 1e-6
+        assert abs(res[name][2][13] - res[name][1][13]) <= 2.0 * drift64
+        assert res[name][2][14] <= 2.0 * gw64 and res[name][2][16] <= 2.0 * gy64
         np.testing.assert_allclose(res[name][3]["mean"][m], s64[m], rtol=1e-4)
 
 

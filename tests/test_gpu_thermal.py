@@ -12,6 +12,10 @@ the checks are the ones a random field allows:
   constraint columns of the snapshot row vanish);
 - momenta are zero;
 - a seed fixes the state (any form, any member of an ensemble).
+Besides: the reference's own construction from given deviates
+(ewpt_init_thermal_deviates) against the transpiled reference kernels; the
+device Gauss projection (ewpt_gauss_project) against the host one; and the
+projected thermal IC (ewpt_init_thermal_gauss) against the constraint bars.
 """
 import dataclasses
 import math
@@ -173,3 +177,43 @@ def test_device_thermal_from_deviates_matches_reference_kernels(golden_dir, prec
     scale = np.abs(ref[:16]).max(axis=1, keepdims=True)
     assert (np.abs(y[:16] - ref[:16]) / scale).max() < 1e-12
     assert np.abs(y[16:]).max() == 0.0
+
+
+@pytest.mark.parametrize("shape", [(16, 14, 18), (15, 16, 17)])
+def test_device_gauss_projection_matches_host(shape):
+    """ewpt_gauss_project against ewpt/ic.py gauss_project on the same
+    unprojected thermal state (fields and momenta drawn, no projection):
+    after 6 iterations the Higgs momenta and electric fields agree to 1e-9 of
+    each array's largest value (cuFFT D2Z/Z2D and a Jacobi SVD against
+    numpy's complex FFT and lstsq); every other array is untouched."""
+    p = ewpt.baseline_couplings(shape=shape, N=shape[0], dx=0.25, dt=0.025)
+    y0 = ic.thermal(shape, p.dx, T=1.5, gw=p.gw, gy=p.gy, seed=12, gauss_iters=0, with_momenta=True)
+    yh = ic.gauss_project(y0.copy(), shape, p.dx, p.gw, p.gy, iters=6)
+    with ewpt.Lattice(p) as lat:
+        lat.set_state(y0)
+        lat.gauss_project(6)
+        yd = lat.get_state()
+    np.testing.assert_array_equal(yd[:20], y0[:20])
+    scale = np.abs(yh[20:]).max(axis=1, keepdims=True)
+    assert (np.abs(yd[20:] - yh[20:]) / scale).max() < 1e-9
+
+
+@pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32, ewpt.DF64])
+def test_init_thermal_gauss_meets_the_constraints(prec):
+    """ewpt_init_thermal_gauss: 20 projection iterations leave the U(1)
+    Gauss violation below 1e-10 and the SU(2) one below 1e-6 of the
+    unprojected state's (the host projection's bars); Gamma = div W holds
+    and the momenta are the thermal ones, not zero."""
+    shape = (32, 32, 32)
+    p = ewpt.baseline_couplings(shape=shape, N=32, dx=0.25, dt=0.025, precision=prec)
+    with ewpt.Lattice(p) as lat:
+        lat.init_thermal_gauss(1.5, seed=21, gauss_iters=0)
+        d0 = lat.diagnostics()
+        lat.init_thermal_gauss(1.5, seed=21, gauss_iters=20)
+        d1 = lat.diagnostics()
+        y = lat.get_state()
+    assert d0[14] > 1.0 and d0[16] > 1.0
+    assert d1[16] < 1e-10 * d0[16]
+    assert d1[14] < 1e-6 * d0[14]
+    assert d1[18] < 1e-9 and d1[19] < 1e-9  # Gamma = div W, Sigma = div Y
+    assert np.abs(y[20:]).max() > 0.0

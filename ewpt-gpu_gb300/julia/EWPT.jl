@@ -125,4 +125,127 @@ function rk4_step!(p::Params, inputs::Vector{Ptr{Float64}}, outputs::Vector{Ptr{
                 p, inputs, outputs, Jex, γ, stream))
 end
 
+"""Launch shape of the stage kernels (ewpt_set_tiling): bx x by threads,
+register variant `reg`, `pair` = 1 two sites per thread (FP32 form), 2 TMA tiles."""
+set_tiling!(L::Lattice, bx, by; reg=0, pair=0) =
+    check(ccall((:ewpt_set_tiling, libewpt), Cint, (Ptr{Cvoid}, Int32, Int32, Int32, Int32), L.h, bx, by, reg, pair), L.h)
+
+"""Bubble IC on the device (ewpt_init_bubbles; replaces the per-bubble
+`initializer!` launches, main_rk4.jl:4930-4946, :5691-5697).  `bubbles` is
+7 x nb: centre (1-based site indices for profile 0, physical units for
+profile 1), then the direction d1..d4; profile 0 = the reference's rmag
+profile, 1 = tanh with radius p0 and wall width p1."""
+function init_bubbles!(L::Lattice, bubbles::Matrix{Float64}; profile=0, p0=0.0, p1=0.0)
+    size(bubbles, 1) == 7 || error("bubbles must be 7 x nb")
+    check(ccall((:ewpt_init_bubbles, libewpt), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Int32, Float64, Float64),
+                L.h, size(bubbles, 2), bubbles, profile, p0, p1), L.h)
+end
+
+"""The 44 deviate arrays of run()'s thermal branch (main_rk4.jl:5348-5636),
+drawn exactly as run() draws them: `Random.seed!(seed_value * iter);
+rand(Normal(0.0, sqrt(2.0)), (Nx, Ny, Nz))` with iter = 5, 6, ... for W^1,
+W^2, W^3 and Y (r_1, r_2, r_3, r_1_i, r_2_i, r_3_i, x_1 .. x_4 each), then
+phi_1_k .. phi_4_k with seeds seed_value * 1 .. 4.  `normal` is the
+sampler, e.g. `(dims) -> rand(Normal(0.0, sqrt(2.0)), dims)` from
+Distributions (the reference's own dependency).  Returns an
+(Nx, Ny, Nz, 44) array, the layout init_thermal_deviates! takes."""
+function reference_deviates(p::Params, seed_value::Integer, normal, seed!)
+    Nx, Ny, Nz = Int(p.nx), Int(p.ny), Int(p.nz)
+    d = Array{Float64}(undef, Nx, Ny, Nz, 44)
+    iter = 5
+    for q in 1:40
+        seed!(seed_value * iter)
+        d[:, :, :, q] = normal((Nx, Ny, Nz))
+        iter += 1
+    end
+    for a in 1:4
+        seed!(seed_value * a)
+        d[:, :, :, 40 + a] = normal((Nx, Ny, Nz))
+    end
+    d
+end
+
+"""The reference's thermal IC from given deviates (ewpt_init_thermal_deviates):
+thermal_initializer_gauge!/phi! + bfft (main_rk4.jl:5029-5152) on the device.
+The reference's own conventions are the defaults: mH^2 = meff_sq
+(parameters.jl:37), massless gauge modes, 1-based mode indices."""
+function init_thermal_deviates!(L::Lattice, T, deviates::Array{Float64,4}; mH=sqrt(8119.43 / 174.0^2), mW=0.0,
+                                one_based=true)
+    size(deviates) == (L.p.nx, L.p.ny, L.p.nz, 44) || error("deviates must be (nx, ny, nz, 44)")
+    check(ccall((:ewpt_init_thermal_deviates, libewpt), Cint,
+                (Ptr{Cvoid}, Float64, Float64, Float64, Ptr{Float64}, Int32, Int32),
+                L.h, T, mH, mW, deviates, 0, one_based ? 1 : 0), L.h)
+end
+
+"""Thermal IC with Gauss-projected thermal momenta (ewpt_init_thermal_gauss)."""
+function init_thermal_gauss!(L::Lattice, T; seed::Integer=0, gauss_iters=20, mH=sqrt(2 * L.p.lambda) * L.p.vev,
+                             mW=L.p.gw * L.p.vev / 2)
+    check(ccall((:ewpt_init_thermal_gauss, libewpt), Cint, (Ptr{Cvoid}, Float64, Float64, Float64, UInt64, Int32),
+                L.h, T, mH, mW, UInt64(seed), gauss_iters), L.h)
+end
+
+"""Project the state's electric fields onto the Gauss law (ewpt_gauss_project)."""
+gauss_project!(L::Lattice; iters=20) =
+    check(ccall((:ewpt_gauss_project, libewpt), Cint, (Ptr{Cvoid}, Int32), L.h, iters), L.h)
+
+"""A lattice cut into z-slabs (ewpt_slabs_create): the decomposition of
+main_rk4_multiple.jl (update_halo!, boundary_x/y/z, :69-212) in one process,
+slab m on devices[m]; `nz_local` planes per slab (default an even split)."""
+mutable struct Slabs
+    h::Ptr{Cvoid}
+    p::Params
+end
+function Slabs(p::Params, n::Integer; nz_local=nothing, devices=nothing)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    nzl = nz_local === nothing ? C_NULL : Int32.(nz_local)
+    dev = devices === nothing ? C_NULL : Int32.(devices)
+    rc = ccall((:ewpt_slabs_create, libewpt), Cint, (Ref{Params}, Int32, Ptr{Int32}, Ptr{Int32}, Ref{Ptr{Cvoid}}),
+               p, n, nzl, dev, r)
+    check(rc)
+    s = Slabs(r[], p)
+    finalizer(x -> ccall((:ewpt_slabs_destroy, libewpt), Cint, (Ptr{Cvoid},), x.h), s)
+    s
+end
+slabs_check(rc, s::Slabs) = rc == 0 ? nothing :
+    error("libewpt error $rc: " * unsafe_string(ccall((:ewpt_slabs_last_error, libewpt), Cstring, (Ptr{Cvoid},), s.h)))
+"""Whole-lattice state, packed (nx, ny, nz, 36) on the host."""
+set_state!(s::Slabs, y::Array{Float64,4}) =
+    slabs_check(ccall((:ewpt_slabs_set_state, libewpt), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32), s.h, y, 0), s)
+function get_state(s::Slabs)
+    y = Array{Float64}(undef, s.p.nx, s.p.ny, s.p.nz, 36)
+    slabs_check(ccall((:ewpt_slabs_get_state, libewpt), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32), s.h, y, 0), s)
+    y
+end
+step!(s::Slabs, nsteps::Integer=1) =
+    slabs_check(ccall((:ewpt_slabs_step, libewpt), Cint, (Ptr{Cvoid}, Int32), s.h, nsteps), s)
+
+"""A batched ensemble of FP32-form members (ewpt_ensemble_create): `members`
+is a vector of Params, one per realization."""
+mutable struct Ensemble
+    h::Ptr{Cvoid}
+    members::Vector{Params}
+end
+function Ensemble(members::Vector{Params})
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:ewpt_ensemble_create, libewpt), Cint, (Int32, Ptr{Params}, Ref{Ptr{Cvoid}}),
+                length(members), members, r))
+    e = Ensemble(r[], members)
+    finalizer(x -> ccall((:ewpt_ensemble_destroy, libewpt), Cint, (Ptr{Cvoid},), x.h), e)
+    e
+end
+ens_check(rc, e::Ensemble) = rc == 0 ? nothing :
+    error("libewpt error $rc: " * unsafe_string(ccall((:ewpt_ensemble_last_error, libewpt), Cstring,
+                                                      (Ptr{Cvoid},), e.h)))
+"""Member m (0-based) from a packed (nx, ny, nz, 36) host state."""
+set_state!(e::Ensemble, m::Integer, y::Array{Float64,4}) =
+    ens_check(ccall((:ewpt_ensemble_set_state, libewpt), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Int32),
+                    e.h, m, y, 0), e)
+step!(e::Ensemble, nsteps::Integer=1) =
+    ens_check(ccall((:ewpt_ensemble_step, libewpt), Cint, (Ptr{Cvoid}, Int32), e.h, nsteps), e)
+function diagnostics(e::Ensemble, m::Integer)
+    out = zeros(Float64, 20)
+    ens_check(ccall((:ewpt_ensemble_diagnostics, libewpt), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}), e.h, m, out), e)
+    out
+end
+
 end # module

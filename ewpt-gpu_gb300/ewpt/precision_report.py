@@ -13,10 +13,13 @@ reference here: it matches the CPU oracle to 1e-11 per field over 100 steps
 
 `--device-ic` starts every form from the device thermal IC instead
 (ewpt_init_thermal with the seed: the reference's construction, momenta
-zero, generated in milliseconds at any size).  `--gauss-iters` sets the
-fixed-point iterations of the host IC's Gauss projection of the initial
-electric fields (each one removes about half of the remaining
-constraint residual; 20 leave ~1e-7 of the charge density).  `--forms`
+zero, generated in milliseconds at any size).  `--device-gauss` starts
+every form from the device IC of the precision configuration
+(ewpt_init_thermal_gauss: thermal fields and momenta, the momenta projected
+onto the Gauss law on the device with `--gauss-iters` iterations).
+`--gauss-iters` sets the iterations of the Gauss projection (host IC:
+fixed-point iterations, each removing about half of the remaining
+constraint residual, 20 leave ~1e-7 of the charge density).  `--forms`
 picks the forms; fp64 always runs, as the reference.
 
 `--control EPS` adds the control run "fp64_perturbed": the FP64 form from
@@ -54,7 +57,9 @@ def evolve(p, y0, steps, every, tune=True, perturb=0.0, perturb_seed=11):
     # the sweep runs on its own scratch lattice: pick the shape before this one exists
     tile = autotune.best_tiling(p) if tune else None
     with Lattice(p) as lat:
-        if isinstance(y0, tuple):
+        if isinstance(y0, tuple) and y0[0] == "device-gauss":
+            lat.init_thermal_gauss(y0[1], seed=y0[2], gauss_iters=y0[3])
+        elif isinstance(y0, tuple):
             lat.init_thermal(y0[1], seed=y0[2])
         else:
             lat.set_state(y0)
@@ -91,10 +96,15 @@ FORMS = {"fp64": _lib.FP64, "fp32": _lib.FP32, "df64": _lib.DF64}
 
 
 def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df64"), gauss_iters=20,
-           device_ic=False, control=0.0):
+           device_ic=False, control=0.0, device_gauss=False):
     shape = (N, N, N)
     t0 = time.perf_counter()
-    y0 = ("device", T, seed) if device_ic else ic.thermal(shape, 0.25, T=T, seed=seed, gauss_iters=gauss_iters)
+    if device_gauss:
+        y0 = ("device-gauss", T, seed, gauss_iters)
+    elif device_ic:
+        y0 = ("device", T, seed)
+    else:
+        y0 = ic.thermal(shape, 0.25, T=T, seed=seed, gauss_iters=gauss_iters)
     t_ic = time.perf_counter() - t0
     runs = {}
     names = ["fp64"] + [f for f in forms if f != "fp64"] + (["fp64_perturbed"] if control else [])
@@ -109,7 +119,9 @@ def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df
     E0 = ref["hist"][0, 1]
     smask = ref["spec"] > 1e-12 * ref["spec"].max()
     out = dict(lattice=list(shape), steps=steps, every=every, T=T, seed=seed, dt=0.025, dx=0.25,
-               ic="device (momenta zero)" if device_ic else f"host (Gauss projection, {gauss_iters} iterations)",
+               ic=(f"device (thermal momenta, Gauss projection on the device, {gauss_iters} iterations)"
+                   if device_gauss else "device (momenta zero)" if device_ic
+                   else f"host (Gauss projection, {gauss_iters} iterations)"),
                ic_seconds=t_ic, control_perturbation=control, forms={})
     for name, r in runs.items():
         h = r["hist"]
@@ -138,6 +150,8 @@ def main(argv=None):
     ap.add_argument("--gauss-iters", type=int, default=20)
     ap.add_argument("--device-ic", action="store_true",
                     help="the device thermal IC (ewpt_init_thermal: the reference's construction, momenta zero)")
+    ap.add_argument("--device-gauss", action="store_true",
+                    help="the device IC with thermal momenta projected onto the Gauss law (ewpt_init_thermal_gauss)")
     ap.add_argument("--control", type=float, default=0.0,
                     help="relative size of the perturbed-IC FP64 control run (0: none)")
     ap.add_argument("--out", default=None)
@@ -146,7 +160,7 @@ def main(argv=None):
     bad = [f for f in forms if f not in FORMS]
     if bad:
         ap.error(f"unknown forms {bad}; choose from {sorted(FORMS)}")
-    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters, a.device_ic, a.control)
+    r = report(a.N, a.steps, a.every, a.T, a.seed, forms, a.gauss_iters, a.device_ic, a.control, a.device_gauss)
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:

@@ -96,6 +96,7 @@ def _sig(L):
     L.ewpt_ensemble_set_drive.argtypes = [E, C.c_int32, C.c_double, C.c_double]
     L.ewpt_ensemble_init_thermal.argtypes = [E, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64]
     L.ewpt_ensemble_set_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32]
+    L.ewpt_ensemble_set_member_tiling.argtypes = [E, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.ewpt_ensemble_step.argtypes = [E, C.c_int32]
     L.ewpt_ensemble_sync.argtypes = [E]
     L.ewpt_ensemble_stream.argtypes = [E]

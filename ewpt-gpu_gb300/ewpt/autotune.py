@@ -21,7 +21,9 @@ CANDIDATES = [(32, 4, 0, 0), (64, 2, 0, 0), (32, 2, 0, 0), (16, 8, 0, 0), (128, 
               (32, 4, 2, 0), (64, 2, 2, 0), (32, 2, 2, 0), (16, 8, 2, 0)]
 # FP32 form only: two sites per thread (needs even nx)
 PAIR_CANDIDATES = [(32, 4, 0, 1), (64, 2, 0, 1), (32, 2, 0, 1), (16, 4, 0, 1), (32, 1, 0, 1), (64, 1, 0, 1),
-                   (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1)]
+                   (32, 4, 1, 1), (64, 2, 1, 1), (32, 2, 1, 1), (32, 4, 2, 1), (64, 2, 2, 1), (32, 2, 2, 1),
+                   # narrow blocks for lattices of 48-160 sites per row (ensemble members)
+                   (16, 8, 2, 1), (8, 16, 2, 1), (16, 8, 0, 1)]
 # FP32 form only: TMA-staged tiles of 32 x by x bz sites, (bx, by, bz, 2)
 TMA_CANDIDATES = [(32, 4, 4, 2), (32, 2, 4, 2)]
 
@@ -129,6 +131,39 @@ def tune(lat: Lattice, steps: int = 2) -> tuple:
 # waste fewer threads on members of 48 / 96 / 160 sites per row
 ENSEMBLE_CANDIDATES = [(8, 8, 1), (8, 16, 1), (16, 8, 1), (16, 4, 1), (8, 4, 1), (32, 4, 1), (32, 2, 1), (64, 2, 1),
                        (32, 4, 0), (16, 8, 0), (32, 2, 0)]
+
+
+def member_tilings(members, steps: int = 2, use_cache: bool = True) -> list:
+    """The fastest single-lattice launch shape (one site or two sites per
+    thread; the ensemble's graph branches run those kernels) for each member,
+    timed once per distinct member size and couplings switch and cached."""
+    out, seen = [], {}
+    for p in members:
+        even = p.dims[0] % 2 == 0
+        cands = list(CANDIDATES) + (list(PAIR_CANDIDATES) if even else [])
+        key = "member:" + _key(p)
+        if key not in seen:
+            cache = _load_cache() if use_cache else {}
+            if key in cache:
+                seen[key] = tuple(cache[key]["tile"])
+            else:
+                res = sweep(p, steps, cands)
+                tile, t = min(res, key=lambda r: r[1])
+                cache[key] = {"tile": list(tile), "s_per_step": t, "sweep": [[list(a), b] for a, b in res]}
+                if use_cache:
+                    _save_cache(cache)
+                seen[key] = tile
+        out.append(seen[key])
+    return out
+
+
+def tune_ensemble(ens, steps: int = 2) -> list:
+    """Apply member_tilings to a live ensemble (the sweeps run on scratch
+    lattices of the members' sizes); returns the shapes."""
+    tiles = member_tilings(ens.members, steps)
+    for m, t in enumerate(tiles):
+        ens.set_member_tiling(m, *t)
+    return tiles
 
 
 def best_ensemble_tiling(members, steps: int = 2, use_cache: bool = True) -> tuple:

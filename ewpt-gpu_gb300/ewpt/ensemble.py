@@ -1,6 +1,6 @@
-"""Batched ensemble of independent lattices (FP32 form), one persistent
-kernel launch per RK4 stage over all members, stages replayed from a CUDA
-graph (ewpt_ensemble_* in include/ewpt.h)."""
+"""Batched ensemble of independent lattices (FP32 form): every member a
+single-lattice FP32 context, one step of all members one CUDA graph with a
+concurrent branch per member (ewpt_ensemble_* in include/ewpt.h)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -96,6 +96,10 @@ class Ensemble:
 
     def set_tiling(self, bx: int, by: int, pair: int):
         self._chk(self.L.ewpt_ensemble_set_tiling(self.h, bx, by, pair))
+
+    def set_member_tiling(self, m: int, bx: int, by: int, reg: int = 2, pair: int = 1):
+        """Launch shape of member m alone (as Lattice.set_tiling, pair 0 or 1)."""
+        self._chk(self.L.ewpt_ensemble_set_member_tiling(self.h, int(m), int(bx), int(by), int(reg), int(pair)))
 
     def step(self, n: int = 1):
         self._chk(self.L.ewpt_ensemble_step(self.h, int(n)))

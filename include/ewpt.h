@@ -312,11 +312,12 @@ int ewpt_slab_stage(ewpt_ctx* ctx, int32_t stage, double Jex, double gamma);
 /* ---------------------------------------------------------------------
  * Batched ensembles (no counterpart in the reference, which runs one
  * realization per process; each member here is an independent lattice with
- * its own size, couplings and dt, in the FP32 form).  One RK4 stage over all
- * members is one persistent kernel launch; the four stages of a step are
- * replayed from a CUDA graph.  Member m evolves exactly like a single
- * FP32-form context with the same paired/scalar mode.  Members start at
- * zero and carry per-member Jex/gamma (default 0, see ewpt_ensemble_set_drive).
+ * its own size, couplings and dt, in the FP32 form).  Every member is an
+ * FP32-form context evolved by the single-lattice stage kernels, so member m
+ * evolves exactly like a single context with the same tiling.  One RK4 step
+ * of all members is one CUDA graph with a branch per member; the branches
+ * run concurrently on the GPU.  Members start at zero and carry per-member
+ * Jex/gamma (default 0, see ewpt_ensemble_set_drive).
  */
 typedef struct ewpt_ens ewpt_ens;
 int ewpt_ensemble_create(int32_t n, const ewpt_params* members, ewpt_ens** out);
@@ -339,10 +340,13 @@ int ewpt_ensemble_init_thermal_gauss(ewpt_ens* ens, int32_t m, double T, double 
                                      int32_t gauss_iters);
 /* constant Jex and gamma of member m for the following steps */
 int ewpt_ensemble_set_drive(ewpt_ens* ens, int32_t m, double Jex, double gamma);
-/* launch shape: bx*by threads (whole warps, <= 128), pair = two x-adjacent
- * sites per thread (every member needs an even nx; default when possible).
- * Default 8x8 threads. */
+/* launch shape of every member: bx*by threads (whole warps, <= 128), at
+ * most 168 registers, pair = two x-adjacent sites per thread (every member
+ * needs an even nx; default when possible).  Default 16x8 threads. */
 int ewpt_ensemble_set_tiling(ewpt_ens* ens, int32_t bx, int32_t by, int32_t pair);
+/* launch shape of member m alone, as ewpt_set_tiling (pair 0 or 1), e.g.
+ * the shape a single lattice of that size runs fastest with */
+int ewpt_ensemble_set_member_tiling(ewpt_ens* ens, int32_t m, int32_t bx, int32_t by, int32_t reg, int32_t pair);
 /* nsteps RK4 steps of every member, asynchronous on the ensemble's stream */
 int ewpt_ensemble_step(ewpt_ens* ens, int32_t nsteps);
 int ewpt_ensemble_sync(ewpt_ens* ens);

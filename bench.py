@@ -48,10 +48,10 @@ BYTES_FP32 = 2592  # y in FP64 width, stage rates in FP32
 # DRAM bytes per site-update (sum over the 4 stage launches) from one ncu
 # capture of the stage kernels (dram__bytes_read.sum + dram__bytes_write.sum):
 # FP64 at 80^3, 32x2 threads; FP32 form at 128^3, the tuned paired kernel
-# (64x2 pair-threads, <= 168 registers).  Traffic grows with the site count,
+# (64x2 pair-threads, <= 168 registers, with its L2 prefetches).  Traffic grows with the site count,
 # so a 256^3 launch moves this x S / 4.
 TRAFFIC_FP64 = 4383
-TRAFFIC_FP32 = 2804
+TRAFFIC_FP32 = 2973
 # FP64 operations of one site-update of the FP64 stage kernels (4 stages of
 # site_rates + the RK4 epilogue), counted exactly by compiling the kernels'
 # own per-site templates with an operator-counting scalar type

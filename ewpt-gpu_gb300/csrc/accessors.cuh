@@ -132,13 +132,25 @@ struct SiteAcc {
 // stencil reads the aligned pairs at i0-4, i0-2, i0, i0+2, i0+4 and re-pairs
 // them into the +-1, +-2, +-3 neighbours; y and z neighbours are aligned
 // pairs of the same x columns.  Needs nx even.
-template <class Src>
+//
+// COMP = true (the FP32 form's compensated mode) adds grad_lap_c / grad_c:
+// the Laplacian and the gradient as unevaluated sums hi + lo, accumulated
+// with error-free transformations from the FP32 stage input and the
+// coefficients split into float pairs (sl holds their low parts), so their
+// error is ~2^-44 of the terms instead of ~2^-24.  The physics takes the
+// gauge fields' Laplacians and the auxiliaries' gradients this way and
+// subtracts them (comp_diff) before rounding to FP32: for the longitudinal
+// gauge modes the two nearly cancel, and FP32 rounding of each would leak
+// into the transverse (magnetic) modes.
+template <class Src, bool COMP = false>
 struct PairAcc {
+    static constexpr bool kCompGauge = COMP;
     Src src;
     int c;      // linear index of site i0 (even)
     int ox[4];  // float offsets of the x pairs at i0-4, i0-2, i0+2, i0+4 (wrapped)
     int oy[6], oz[6];
     StencilCoef<f2> s;
+    StencilCoef<f2> sl;  // low parts of the coefficients (COMP only)
 
     __device__ __forceinline__ float2 ld(int a, int off) const {
         return __ldg(reinterpret_cast<const float2*>(src.arr(a) + (c + off)));
@@ -195,6 +207,100 @@ struct PairAcc {
     }
     __device__ __forceinline__ f2 div3(int a) const { return dx(a) + d1(a + 1, oy) + d1(a + 2, oz); }
 
+    // ---- compensated stencils (COMP)
+    // (sh, sl) += v
+    __device__ __forceinline__ static void acc2(f2& sh, f2& slo, const f2& v) {
+        f2 e;
+        two_sum2(sh, v, sh, e);
+        slo = slo + e;
+    }
+    // (h, l) = coefficient (ch + cl) times (xh + xl), to ~2^-44
+    __device__ __forceinline__ static void mul_c(const f2& ch, const f2& cl, const f2& xh, const f2& xl, f2& h, f2& l) {
+        two_prod2(ch, xh, h, l);
+        l = l + ch * xl + cl * xh;
+    }
+    // the plain gradient and the compensated Laplacian (lh + ll)
+    __device__ __forceinline__ void grad_lap_c(int a, f2& gx, f2& gy, f2& gz, f2& lh, f2& ll) const {
+        f2 Sh[3], Sl[3];  // sum over the axes of (f(+k) + f(-k)), k = 1, 2, 3
+        {
+            f2 p1, p2, p3, m1, m2, m3;
+            xpairs(a, p1, p2, p3, m1, m2, m3);
+            gx = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            two_sum2(p1, m1, Sh[0], Sl[0]);
+            two_sum2(p2, m2, Sh[1], Sl[1]);
+            two_sum2(p3, m3, Sh[2], Sl[2]);
+        }
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            const int* o = ax == 0 ? oy : oz;
+            const f2 p1 = f2(ld(a, o[0])), p2 = f2(ld(a, o[1])), p3 = f2(ld(a, o[2]));
+            const f2 m1 = f2(ld(a, o[3])), m2 = f2(ld(a, o[4])), m3 = f2(ld(a, o[5]));
+            const f2 g = s.a1 * (p1 - m1) + s.a2 * (p2 - m2) + s.a3 * (p3 - m3);
+            if (ax == 0)
+                gy = g;
+            else
+                gz = g;
+            acc2(Sh[0], Sl[0], p1);
+            acc2(Sh[0], Sl[0], m1);
+            acc2(Sh[1], Sl[1], p2);
+            acc2(Sh[1], Sl[1], m2);
+            acc2(Sh[2], Sl[2], p3);
+            acc2(Sh[2], Sl[2], m3);
+        }
+        // l0 f0 + l1 S1 + l2 S2 + l3 S3
+        const f2 f0 = v(a);
+        two_prod2(s.l0, f0, lh, ll);
+        ll = ll + sl.l0 * f0;
+        const f2 ch[3] = {s.l1, s.l2, s.l3}, cl[3] = {sl.l1, sl.l2, sl.l3};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            f2 th, tl, e;
+            mul_c(ch[k], cl[k], Sh[k], Sl[k], th, tl);
+            two_sum2(lh, th, lh, e);
+            ll = ll + (tl + e);
+        }
+    }
+    // the compensated derivative along one axis from its six neighbour pairs
+    __device__ __forceinline__ void d1_c(const f2& p1, const f2& p2, const f2& p3, const f2& m1, const f2& m2,
+                                         const f2& m3, f2& h, f2& l) const {
+        const f2 ah[3] = {s.a1, s.a2, s.a3}, al[3] = {sl.a1, sl.a2, sl.a3};
+        const f2 p[3] = {p1, p2, p3}, m[3] = {m1, m2, m3};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            f2 dh, dl, th, tl;
+            two_sum2(p[k], -m[k], dh, dl);
+            mul_c(ah[k], al[k], dh, dl, th, tl);
+            if (k == 0) {
+                h = th;
+                l = tl;
+            } else {
+                f2 e;
+                two_sum2(h, th, h, e);
+                l = l + (tl + e);
+            }
+        }
+    }
+    // compensated gradient: gh[i] + gl[i]
+    __device__ __forceinline__ void grad_c(int a, f2* gh, f2* gl) const {
+        {
+            f2 p1, p2, p3, m1, m2, m3;
+            xpairs(a, p1, p2, p3, m1, m2, m3);
+            d1_c(p1, p2, p3, m1, m2, m3, gh[0], gl[0]);
+        }
+#pragma unroll
+        for (int ax = 0; ax < 2; ++ax) {
+            const int* o = ax == 0 ? oy : oz;
+            d1_c(f2(ld(a, o[0])), f2(ld(a, o[1])), f2(ld(a, o[2])), f2(ld(a, o[3])), f2(ld(a, o[4])),
+                 f2(ld(a, o[5])), gh[ax + 1], gl[ax + 1]);
+        }
+    }
+    // (xh + xl) - (yh + yl), rounded once
+    __device__ __forceinline__ static f2 comp_diff(const f2& xh, const f2& xl, const f2& yh, const f2& yl) {
+        f2 d, e;
+        two_sum2(xh, -yh, d, e);
+        return d + (e + (xl - yl));
+    }
+
     __device__ __forceinline__ void place(int i0, int j, int k, int nx, int ny, int nz) {
         c = i0 + nx * (j + ny * k);
         ox[0] = (i0 - 4 >= 0 ? -4 : nx - 4);
@@ -225,6 +331,11 @@ struct PairAcc {
 template <typename T>
 __host__ __device__ inline StencilCoef<f2> pair_stencil(const StencilCoef<T>& s) {
     return StencilCoef<f2>{f2(s.a1), f2(s.a2), f2(s.a3), f2(s.l0), f2(s.l1), f2(s.l2), f2(s.l3)};
+}
+// the parts the FP32 coefficients miss: c - (float)c of the FP64 coefficients
+inline StencilCoef<f2> pair_stencil_lo(const StencilCoef<double>& d) {
+    auto lo = [](double x) { return f2((float)(x - (double)(float)x)); };
+    return StencilCoef<f2>{lo(d.a1), lo(d.a2), lo(d.a3), lo(d.l0), lo(d.l1), lo(d.l2), lo(d.l3)};
 }
 
 // Compensated accumulation (hi, lo) += p (TwoSum, then renormalise).

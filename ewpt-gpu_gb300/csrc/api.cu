@@ -3,6 +3,7 @@
 // A context owns the device state of one periodic lattice and one CUDA
 // stream.  Host <-> device copies are explicit (ewpt_set_state /
 // ewpt_get_state); stepping, diagnostics and spectra run on the stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -186,6 +187,10 @@ int ewpt_destroy(ewpt_ctx* c) {
     cudaFree(c->w32.xa);
     cudaFree(c->w32.xb);
     cudaFree(c->scratch64);
+    for (cudaStream_t s : c->io_st)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : c->io_ev)
+        if (ev) cudaEventDestroy(ev);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return EWPT_OK;
@@ -206,10 +211,43 @@ int ewpt_staging64(ewpt_ctx* c, double** out, bool in) {
 }
 
 // Copy the 36 arrays between the caller's pointers and a [36][S] buffer,
-// one cudaMemcpyAsync per run of arrays that lie back to back in the
-// caller's memory (a packed state is one copy).
-static cudaError_t copy_runs(double* dev, const double* const* arrays, int64_t S, bool to_dev, int32_t on_device,
-                             cudaStream_t st) {
+// Host <-> device copies of a state: one cudaMemcpyAsync per run of arrays
+// that lie back to back in the caller's memory (a packed state is one run).
+// A host run of more than kChunkMin bytes is cut into kChunks pieces copied
+// concurrently on the context's stream and kChunks - 1 side streams (one
+// DMA engine each), joined back into the context's stream by events.
+constexpr int kChunks = 4;
+constexpr size_t kChunkMin = (size_t)64 << 20;
+
+static cudaError_t io_streams(ewpt_ctx* c) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < kChunks - 1 && e == cudaSuccess; ++i)
+        if (!c->io_st[i]) e = cudaStreamCreateWithFlags(&c->io_st[i], cudaStreamNonBlocking);
+    for (int i = 0; i < kChunks && e == cudaSuccess; ++i)
+        if (!c->io_ev[i]) e = cudaEventCreateWithFlags(&c->io_ev[i], cudaEventDisableTiming);
+    return e;
+}
+
+static cudaError_t copy_chunked(ewpt_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    cudaError_t e = io_streams(c);
+    if (e == cudaSuccess) e = cudaEventRecord(c->io_ev[0], c->st);  // fork after the work queued so far
+    const size_t piece = (bytes / kChunks + 4095) & ~(size_t)4095;
+    for (int i = 0; i < kChunks && e == cudaSuccess; ++i) {
+        const size_t off = (size_t)i * piece;
+        if (off >= bytes) break;
+        const size_t n = std::min(piece, bytes - off);
+        cudaStream_t s = i == 0 ? c->st : c->io_st[i - 1];
+        if (i > 0) e = cudaStreamWaitEvent(s, c->io_ev[0], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, n, kind, s);
+        if (e == cudaSuccess && i > 0) e = cudaEventRecord(c->io_ev[i], s);
+        if (e == cudaSuccess && i > 0) e = cudaStreamWaitEvent(c->st, c->io_ev[i], 0);  // join
+    }
+    return e;
+}
+
+static cudaError_t copy_runs(ewpt_ctx* c, double* dev, const double* const* arrays, int64_t S, bool to_dev,
+                             int32_t on_device) {
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice
                                           : (to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
     cudaError_t e = cudaSuccess;
@@ -218,8 +256,10 @@ static cudaError_t copy_runs(double* dev, const double* const* arrays, int64_t S
         while (b < 36 && arrays[b] == arrays[b - 1] + S) ++b;
         const size_t bytes = (size_t)(b - a) * S * 8;
         double* d = dev + (size_t)a * S;
-        e = to_dev ? cudaMemcpyAsync(d, arrays[a], bytes, kind, st)
-                   : cudaMemcpyAsync(const_cast<double*>(arrays[a]), d, bytes, kind, st);
+        void* dst = to_dev ? (void*)d : (void*)const_cast<double*>(arrays[a]);
+        const void* src = to_dev ? (const void*)arrays[a] : (const void*)d;
+        e = (!on_device && bytes > kChunkMin) ? copy_chunked(c, dst, src, bytes, kind)
+                                              : cudaMemcpyAsync(dst, src, bytes, kind, c->st);
         a = b;
     }
     return e;
@@ -235,7 +275,7 @@ int ewpt_set_state(ewpt_ctx* c, const double* const arrays[EWPT_NARR], int32_t o
     double* dst;
     int rc = ewpt_staging64(c, &dst, true);
     if (rc) return rc;
-    cudaError_t e = copy_runs(dst, arrays, c->g.S, true, on_device, c->st);
+    cudaError_t e = copy_runs(c, dst, arrays, c->g.S, true, on_device);
     if (e == cudaSuccess) e = ewpt_commit_staged(c, dst);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     return ewpt_cuda_check(c, e, "set_state");
@@ -260,7 +300,7 @@ int ewpt_get_state(ewpt_ctx* c, double* const arrays[EWPT_NARR], int32_t on_devi
     cudaError_t e = cudaSuccess;
     if (c->p.precision == EWPT_FP32) e = launch_fp32_join(c->g, c->lay, c->y32, src, c->st);
     if (c->p.precision == EWPT_DF64) e = launch_from_dd(36 * c->g.S, c->y, src, c->st);
-    if (e == cudaSuccess) e = copy_runs(src, arrays, c->g.S, false, on_device, c->st);
+    if (e == cudaSuccess) e = copy_runs(c, src, arrays, c->g.S, false, on_device);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     rc = ewpt_cuda_check(c, e, "get_state");
     return rc ? rc : ewpt_tma_check(c);
@@ -326,7 +366,7 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
             e = launch_step_fp32_tma(c, J, G);
         else
             e = (c->tile.pair && c->g.nx % 2 == 0)
-                    ? launch_step_fp32_pair(c->g, c->lay, c->tile, c->y32, c->w32, c->p, J, G, c->st)
+                    ? launch_step_fp32_pair(c->g, c->lay, c->tile, c->y32, c->w32, c->p, J, G, c->st, c->fp32_comp)
                     : launch_step_fp32(c->g, c->lay, c->tile, c->y32, c->w32, c->p, J, G, c->st);
         int rc = ewpt_cuda_check(c, e, "step launch");
         if (rc) return rc;
@@ -343,8 +383,21 @@ int ewpt_step_explicit(ewpt_ctx* c, int32_t nsteps, double Jex, double gamma) {
 
 int64_t ewpt_iteration(const ewpt_ctx* c) { return c ? c->it : -1; }
 
+int ewpt_set_fp32_compensated(ewpt_ctx* c, int32_t on) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (c->p.precision != EWPT_FP32) return ewpt_fail(c, EWPT_ERR_ARG, "the compensated mode is an FP32-form mode");
+    if (on && (c->tile.pair != 1 || c->g.nx % 2 != 0))
+        return ewpt_fail(c, EWPT_ERR_ARG, "the compensated mode runs two sites per thread: set a tiling with pair = 1");
+    c->fp32_comp = on != 0;
+    return EWPT_OK;
+}
+
+int32_t ewpt_get_fp32_compensated(const ewpt_ctx* c) { return c && c->fp32_comp ? 1 : 0; }
+
 int ewpt_set_tiling(ewpt_ctx* c, int32_t bx, int32_t by, int32_t reg, int32_t pair) {
     if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (c->fp32_comp && pair != 1)
+        return ewpt_fail(c, EWPT_ERR_ARG, "the compensated mode runs two sites per thread (pair = 1)");
     if (pair == 2) {
         // TMA-staged shared-memory tiles of bx x by x reg sites (FP32 form)
         if (bx != 32 || (by != 2 && by != 4) || reg != 4)

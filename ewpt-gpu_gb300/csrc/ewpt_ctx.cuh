@@ -30,6 +30,10 @@ struct ewpt_ctx {
     void* tma = nullptr;  // TMA stage-kernel state (stage_tma.cu), made by the first TMA tiling
     int64_t wait_polls = -1;  // limit of the TMA kernels' mbarrier waits in polls (< 0: default)
     Fp32Work w32{nullptr, nullptr, nullptr};
+    bool fp32_comp = false;  // FP32 form: compensated gauge stencils (ewpt_set_fp32_compensated)
+    // side streams and events of the chunked host <-> device state copies (api.cu copy_runs)
+    cudaStream_t io_st[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
     double* scratch64 = nullptr;
     // diagnostics / spectra scratch (diag.cu, spectrum.cu)

@@ -178,8 +178,9 @@ cudaError_t launch_to_dd(int64_t n, double* v, cudaStream_t st);  // in place: d
 cudaError_t launch_from_dd(int64_t n, const double* src, double* dst, cudaStream_t st);
 cudaError_t launch_step_fp32(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
                              const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+// comp: the compensated mode (gauge Laplacians and auxiliary gradients compensated, stage_pair.cu)
 cudaError_t launch_step_fp32_pair(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
-                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st, bool comp = false);
 // Copy the face sites of all 36 arrays of a ghosted buffer into their
 // periodic images (stage.cu); the x faces only if xfaces.
 cudaError_t launch_ghost_fill(const Grid& g, const Layout& L, float* buf, cudaStream_t st, bool xfaces);

@@ -63,3 +63,22 @@ __device__ __forceinline__ f2& f2::operator+=(const f2& b) { return *this = *thi
 __device__ __forceinline__ f2& f2::operator-=(const f2& b) { return *this = *this - b; }
 __device__ __forceinline__ f2& f2::operator+=(const Prod& b) { return *this = *this + b; }
 __device__ __forceinline__ f2& f2::operator-=(const Prod& b) { return *this = *this - b; }
+
+// Error-free transformations on packed pairs (Knuth's TwoSum; the product
+// error by one fused multiply-add), for the compensated stencils of the
+// FP32 form's compensated mode (accessors.cuh PairAcc::grad_lap_c).
+// s + e == a + b exactly (s or e may be the object a or b refers to)
+__device__ __forceinline__ void two_sum2(const f2& a, const f2& b, f2& s, f2& e) {
+    const f2 x = a, y = b;
+    const f2 r = x + y;
+    const f2 bb = r - x;
+    e = (x - (r - bb)) + (y - bb);
+    s = r;
+}
+// p + e == a * b exactly (p or e may be the object a or b refers to)
+__device__ __forceinline__ void two_prod2(const f2& a, const f2& b, f2& p, f2& e) {
+    const f2 x = a, y = b;
+    const f2 r = f2(x * y);
+    e = x * y - r;
+    p = r;
+}

@@ -48,6 +48,17 @@
 #define EWPT_ARITH __device__ __forceinline__
 #endif
 
+#include <type_traits>
+
+// Accessors that declare kCompGauge = true give the gauge fields'
+// Laplacians and the auxiliaries' gradients as compensated pairs
+// (grad_lap_c, grad_c; accessors.cuh PairAcc) and site_rates subtracts them
+// before rounding (comp_diff); every other accessor takes the plain path.
+template <class A, class = void>
+struct CompGauge : std::false_type {};
+template <class A>
+struct CompGauge<A, std::void_t<decltype(A::kCompGauge)>> : std::integral_constant<bool, A::kCompGauge> {};
+
 template <typename T>
 struct PhysCoef {
     T gw, gy, hgw, hgy;  // g, g', g/2, g'/2
@@ -89,6 +100,9 @@ EWPT_ARITH void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
     static_assert(PART == 0 || !BETA, "the beta terms couple every block: PART 0 only");
     constexpr bool kHiggs = PART == 0 || PART == 1, kSU2 = PART == 0 || PART == 2,
                    kRest = PART == 0 || PART == 3;
+    // compensated gauge stencils: kt W^a_i = (lap W^a_i - d_i Gamma^a) + g Q^a_i and
+    // kt Y_i = (lap Y_i - d_i Sigma) + g' jY_i with each bracket formed before rounding
+    constexpr bool kComp = CompGauge<Acc>::value;
     const T gw = c.gw, gy = c.gy, hgw = c.hgw;
     const T p1 = A.v(0), p2 = A.v(1), p3 = A.v(2), p4 = A.v(3);
     T W[3][3];  // W[a][i] = W_{a+1}_{i+2}
@@ -231,11 +245,22 @@ EWPT_ARITH void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
         T dW[3][3];  // dW[i][j] = d_j W^b_i
+        if constexpr (kComp) {
+            T Gh[3], Gl[3];
+            A.grad_c(16 + b, Gh, Gl);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            T lap;
-            A.grad_lap(4 + 3 * b + i, dW[i][0], dW[i][1], dW[i][2], lap);
-            Q[b][i] = Q[b][i] + lap * c.igw;
+            for (int i = 0; i < 3; ++i) {
+                T lh, ll;
+                A.grad_lap_c(4 + 3 * b + i, dW[i][0], dW[i][1], dW[i][2], lh, ll);
+                Q[b][i] = Q[b][i] + A.comp_diff(lh, ll, Gh[i], Gl[i]) * c.igw;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                T lap;
+                A.grad_lap(4 + 3 * b + i, dW[i][0], dW[i][1], dW[i][2], lap);
+                Q[b][i] = Q[b][i] + lap * c.igw;
+            }
         }
         const int b1 = (b + 1) % 3, b2 = (b + 2) % 3;
         F[b][0] = dW[1][0] - dW[0][1] + gw * (W[b1][0] * W[b2][1] - W[b1][1] * W[b2][0]);
@@ -262,11 +287,17 @@ EWPT_ARITH void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
     // the coupling and the auxiliary gradient
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        T gx, gy_, gz;
-        A.grad(16 + a, gx, gy_, gz);
-        ktW[a][0] = gw * Q[a][0] - gx;
-        ktW[a][1] = gw * Q[a][1] - gy_;
-        ktW[a][2] = gw * Q[a][2] - gz;
+        if constexpr (kComp) {  // the gradient is in Q already
+            ktW[a][0] = gw * Q[a][0];
+            ktW[a][1] = gw * Q[a][1];
+            ktW[a][2] = gw * Q[a][2];
+        } else {
+            T gx, gy_, gz;
+            A.grad(16 + a, gx, gy_, gz);
+            ktW[a][0] = gw * Q[a][0] - gx;
+            ktW[a][1] = gw * Q[a][1] - gy_;
+            ktW[a][2] = gw * Q[a][2] - gz;
+        }
     }
 
     }  // SU(2) block
@@ -275,16 +306,33 @@ EWPT_ARITH void site_rates(const Acc& A, const PhysCoef<T>& c, Sink& out) {
     T ktY[3], FY[3];
     if constexpr (kRest) {
         T dY[3][3], lap[3];
+        if constexpr (kComp) {
+            T Sh[3], Sl[3];
+            A.grad_c(19, Sh, Sl);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) A.grad_lap(13 + i, dY[i][0], dY[i][1], dY[i][2], lap[i]);
+            for (int i = 0; i < 3; ++i) {
+                T lh, ll;
+                A.grad_lap_c(13 + i, dY[i][0], dY[i][1], dY[i][2], lh, ll);
+                lap[i] = A.comp_diff(lh, ll, Sh[i], Sl[i]);  // lap Y_i - d_i Sigma
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) A.grad_lap(13 + i, dY[i][0], dY[i][1], dY[i][2], lap[i]);
+        }
         FY[0] = dY[1][0] - dY[0][1];
         FY[1] = dY[2][0] - dY[0][2];
         FY[2] = dY[2][1] - dY[1][2];
-        T gx, gy_, gz;
-        A.grad(19, gx, gy_, gz);
-        ktY[0] = lap[0] + gy * jY[0] - gx;
-        ktY[1] = lap[1] + gy * jY[1] - gy_;
-        ktY[2] = lap[2] + gy * jY[2] - gz;
+        if constexpr (kComp) {
+            ktY[0] = lap[0] + gy * jY[0];
+            ktY[1] = lap[1] + gy * jY[1];
+            ktY[2] = lap[2] + gy * jY[2];
+        } else {
+            T gx, gy_, gz;
+            A.grad(19, gx, gy_, gz);
+            ktY[0] = lap[0] + gy * jY[0] - gx;
+            ktY[1] = lap[1] + gy * jY[1] - gy_;
+            ktY[2] = lap[2] + gy * jY[2] - gz;
+        }
     }
 
     // ---- beta (CP-odd) terms

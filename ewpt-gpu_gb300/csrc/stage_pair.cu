@@ -31,9 +31,9 @@ struct PairBufs {
     float* kacc;
 };
 
-template <int STAGE>
+template <int STAGE, class Acc>
 struct PairSink {
-    const PairAcc<SrcPtr36<float>>& A;
+    const Acc& A;
     const Layout& L;
     PairBufs b;
     float* __restrict__ xn;
@@ -63,20 +63,23 @@ struct PairSink {
 
 __device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-template <int STAGE, bool BETA, int REG>
+// COMP: the compensated mode (gauge Laplacians and auxiliary gradients as
+// compensated pairs, accessors.cuh PairAcc); scl = the coefficients' low parts.
+template <int STAGE, bool BETA, int REG, bool COMP = false>
 __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kMinBlocks)
     k_stage_fp32x2(const __grid_constant__ Grid g, const __grid_constant__ Layout L, const __grid_constant__ Ptr36 X,
                    PairBufs b, float* __restrict__ xn, PhysCoef<f2> pc, StencilCoef<f2> sc, f2 h, f2 w6, int nbx,
-                   int nby, int ycb) {
+                   int nby, int ycb, StencilCoef<f2> scl) {
     int bx, by, k;
     chunk_walk(blockIdx.x, nbx, nby, g.nz, ycb, bx, by, k);
     const int ip = bx * blockDim.x + threadIdx.x;  // pair index along x
     const int j = by * blockDim.y + threadIdx.y;
     const int i0 = 2 * ip;
     if (i0 >= g.nx || j >= g.ny) return;
-    PairAcc<SrcPtr36<float>> A{{X}};
+    PairAcc<SrcPtr36<float>, COMP> A{{X}};
     A.place_ghost(i0, j, k, g.nx, L);
     A.s = sc;
+    A.sl = scl;
     // L2 prefetch of this warp's lines of the epilogue operands (the RK4
     // accumulator and the state, read once each when the rates come out) and
     // of the stage input two planes up (read by the z stencils here and by
@@ -102,7 +105,7 @@ __global__ void __launch_bounds__(PairBudget<REG>::kThreads, PairBudget<REG>::kM
             prefetch_l2(reinterpret_cast<const float*>(X.p[q >> 1]) + cw + kz + 32 * (q & 1));
         }
     }
-    PairSink<STAGE> out{A, L, b, xn, h, w6};
+    PairSink<STAGE, PairAcc<SrcPtr36<float>, COMP>> out{A, L, b, xn, h, w6};
     site_rates<f2, BETA>(A, pc, out);
 }
 
@@ -112,48 +115,53 @@ Ptr36 pack4(const void* base, int64_t S) {
     return P;
 }
 
-template <bool BETA, int REG>
+template <bool BETA, int REG, bool COMP = false>
 void step_pair(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, float* xa, float* xb,
-               const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
+               const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, const StencilCoef<f2>& scl, double dt,
+               cudaStream_t st) {
     const int npx = g.nx / 2;
     const int nbx = (npx + t.bx - 1) / t.bx, nby = (g.ny + t.by - 1) / t.by;
     const int ycb = std::max(1, kChunkRows / t.by);
     const dim3 gr(nbx * nby * g.nz), bl(t.bx, t.by);
     const f2 h2((float)(dt / 2.)), h1((float)dt), w6((float)(dt / 6.)), z(0.f);
-#define EWPT_PAIR_ARGS nbx, nby, ycb
-    k_stage_fp32x2<1, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6, EWPT_PAIR_ARGS);
+#define EWPT_PAIR_ARGS nbx, nby, ycb, scl
+    k_stage_fp32x2<1, BETA, REG, COMP><<<gr, bl, 0, st>>>(g, L, pack4(b.yhi, L.P), b, xa, pc, sc, h2, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32x2<2, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6, EWPT_PAIR_ARGS);
+    k_stage_fp32x2<2, BETA, REG, COMP><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, xb, pc, sc, h2, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xb, st, false);
-    k_stage_fp32x2<3, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6, EWPT_PAIR_ARGS);
+    k_stage_fp32x2<3, BETA, REG, COMP><<<gr, bl, 0, st>>>(g, L, pack4(xb, L.P), b, xa, pc, sc, h1, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, xa, st, false);
-    k_stage_fp32x2<4, BETA, REG><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6, EWPT_PAIR_ARGS);
+    k_stage_fp32x2<4, BETA, REG, COMP><<<gr, bl, 0, st>>>(g, L, pack4(xa, L.P), b, nullptr, pc, sc, z, w6, EWPT_PAIR_ARGS);
     launch_ghost_fill(g, L, b.yhi, st, false);
 #undef EWPT_PAIR_ARGS
 }
 
 template <bool BETA>
 void step_pair_r(const Grid& g, const Layout& L, const Tiling& t, PairBufs b, float* xa, float* xb,
-                 const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, double dt, cudaStream_t st) {
-    if (t.reg == 1)
-        step_pair<BETA, 1>(g, L, t, b, xa, xb, pc, sc, dt, st);
+                 const PhysCoef<f2>& pc, const StencilCoef<f2>& sc, const StencilCoef<f2>& scl, bool comp,
+                 double dt, cudaStream_t st) {
+    if (comp)  // one register budget (<= 168) for the compensated mode
+        step_pair<BETA, 2, true>(g, L, t, b, xa, xb, pc, sc, scl, dt, st);
+    else if (t.reg == 1)
+        step_pair<BETA, 1>(g, L, t, b, xa, xb, pc, sc, scl, dt, st);
     else if (t.reg == 2)
-        step_pair<BETA, 2>(g, L, t, b, xa, xb, pc, sc, dt, st);
+        step_pair<BETA, 2>(g, L, t, b, xa, xb, pc, sc, scl, dt, st);
     else
-        step_pair<BETA, 0>(g, L, t, b, xa, xb, pc, sc, dt, st);
+        step_pair<BETA, 0>(g, L, t, b, xa, xb, pc, sc, scl, dt, st);
 }
 
 }  // namespace
 
 cudaError_t launch_step_fp32_pair(const Grid& g, const Layout& L, const Tiling& t, Fp32State y, Fp32Work w,
-                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+                                  const ewpt_params& p, double Jex, double gam, cudaStream_t st, bool comp) {
     if (g.nx % 2 != 0 || L.gx == 0) return cudaErrorInvalidValue;
     const PhysCoef<f2> pc = make_phys<f2>(p, Jex, gam);
     const StencilCoef<f2> sc = pair_stencil(make_stencil<float>(p.dx));
+    const StencilCoef<f2> scl = pair_stencil_lo(make_stencil<double>(p.dx));
     PairBufs b{y.hi, y.lo, w.kacc};
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        step_pair_r<true>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_pair_r<true>(g, L, t, b, w.xa, w.xb, pc, sc, scl, comp, p.dt, st);
     else
-        step_pair_r<false>(g, L, t, b, w.xa, w.xb, pc, sc, p.dt, st);
+        step_pair_r<false>(g, L, t, b, w.xa, w.xb, pc, sc, scl, comp, p.dt, st);
     return cudaGetLastError();
 }

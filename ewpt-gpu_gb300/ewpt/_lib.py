@@ -121,6 +121,9 @@ def _sig(L):
     L.ewpt_set_tiling.argtypes = [V, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     I32P = C.POINTER(C.c_int32)
     L.ewpt_get_tiling.argtypes = [V, I32P, I32P, I32P, I32P]
+    L.ewpt_set_fp32_compensated.argtypes = [V, C.c_int32]
+    L.ewpt_get_fp32_compensated.argtypes = [V]
+    L.ewpt_get_fp32_compensated.restype = C.c_int32
     L.ewpt_set_wait_limit.argtypes = [V, C.c_int64]
     I32A = C.POINTER(C.c_int32)
     L.ewpt_slabs_create.argtypes = [P, C.c_int32, I32A, I32A, C.POINTER(V)]

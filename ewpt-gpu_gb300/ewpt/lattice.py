@@ -103,6 +103,14 @@ class Lattice:
         """Limit of the TMA-staged kernels' device waits in polls (< 0: default)."""
         self._chk(self.L.ewpt_set_wait_limit(self.h, int(polls)))
 
+    def set_fp32_compensated(self, on: bool = True):
+        """FP32 form: compensated gauge Laplacians and auxiliary gradients
+        (ewpt_set_fp32_compensated); needs a tiling with two sites per thread."""
+        self._chk(self.L.ewpt_set_fp32_compensated(self.h, int(bool(on))))
+
+    def fp32_compensated(self) -> bool:
+        return bool(self.L.ewpt_get_fp32_compensated(self.h))
+
     def tiling(self) -> tuple:
         a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         self._chk(self.L.ewpt_get_tiling(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))

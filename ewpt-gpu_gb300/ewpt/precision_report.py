@@ -13,7 +13,8 @@ reference here: it matches the CPU oracle to 1e-11 per field over 100 steps
 
 `--device-ic` starts every form from the device thermal IC instead
 (ewpt_init_thermal with the seed: the reference's construction, momenta
-zero, generated in milliseconds at any size).  `--device-gauss` starts
+zero, generated in milliseconds at any size).  The form fp32c is the FP32
+form in its compensated mode (ewpt_set_fp32_compensated).  `--device-gauss` starts
 every form from the device IC of the precision configuration
 (ewpt_init_thermal_gauss: thermal fields and momenta, the momenta projected
 onto the Gauss law on the device with `--gauss-iters` iterations).
@@ -49,7 +50,7 @@ from .lattice import Lattice
 from .params import baseline_couplings
 
 
-def evolve(p, y0, steps, every, tune=True, perturb=0.0, perturb_seed=11):
+def evolve(p, y0, steps, every, tune=True, perturb=0.0, perturb_seed=11, comp=False):
     """y0: the (36, S) initial state, or ("device", T, seed) for the device
     thermal IC (identical in every form up to the form's storage).
     perturb: relative size of the seeded perturbation of the initial state."""
@@ -72,6 +73,10 @@ def evolve(p, y0, steps, every, tune=True, perturb=0.0, perturb_seed=11):
             del y
         if tile:
             lat.set_tiling(*tile)
+        if comp:  # the compensated mode runs the two-sites-per-thread kernel
+            if not tile or tile[3] != 1:
+                lat.set_tiling(64, 2, 2, 1)
+            lat.set_fp32_compensated(True)
         d = lat.diagnostics(allow_nonfinite=True)
         hist.append([0, d[13], d[14], d[16]])
         done = 0
@@ -92,7 +97,7 @@ def rel_field_err(a, b):
     return max(float(np.abs(a[q] - b[q]).max() / max(np.abs(b[q]).max(), 1e-300)) for q in range(a.shape[0]))
 
 
-FORMS = {"fp64": _lib.FP64, "fp32": _lib.FP32, "df64": _lib.DF64}
+FORMS = {"fp64": _lib.FP64, "fp32": _lib.FP32, "fp32c": _lib.FP32, "df64": _lib.DF64}
 
 
 def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df64"), gauss_iters=20,
@@ -111,7 +116,7 @@ def report(N=256, steps=500, every=50, T=1.5, seed=7, forms=("fp64", "fp32", "df
     for name in names:
         prec = FORMS["fp64" if name == "fp64_perturbed" else name]
         p = baseline_couplings(N=N, dx=0.25, dt=0.025, precision=prec)
-        r = evolve(p, y0, steps, every, perturb=control if name == "fp64_perturbed" else 0.0)
+        r = evolve(p, y0, steps, every, perturb=control if name == "fp64_perturbed" else 0.0, comp=name == "fp32c")
         if name != "fp64":  # keep one end state besides the reference's (16 GB each at 384^3)
             r["field_err"] = rel_field_err(r.pop("y"), runs["fp64"]["y"])
         runs[name] = r

@@ -10,7 +10,7 @@ fp32x2r2 (k_stage_fp32x2, 64x2 pair-threads, <=168 registers: the tuned 256^3 sh
 (k_stage_tma, TMA-staged 32x4x4-site tiles; N a multiple of 32).  Meant to
 be wrapped by ncu with -k regex:k_stage.  The form ens runs one step of a
 batched ensemble of FP32-form members of 48^3, 96^3, 96^3 and 128^3 (4.0 M
-sites, 2.9 GB; k_ens_stage, 16x8 pair-threads), the member mix of the
+sites; the members' k_stage_fp32x2 launches, 16x8 pair-threads), the member mix of the
 96-member configuration at 1/29 of its size; N is ignored there.
 """
 import argparse

@@ -120,6 +120,19 @@ int64_t ewpt_iteration(const ewpt_ctx* ctx);
  * lattice size and precision.  Default 32x4, 0, 0. */
 int ewpt_set_tiling(ewpt_ctx* ctx, int32_t bx, int32_t by, int32_t reg, int32_t pair);
 int ewpt_get_tiling(const ewpt_ctx* ctx, int32_t* bx, int32_t* by, int32_t* reg, int32_t* pair);
+/* FP32 form, compensated mode (on = 1; default 0): the gauge fields'
+ * Laplacians and the Gauss auxiliaries' gradients are accumulated with
+ * error-free transformations (a float pair, ~2^-44 of the terms) and the
+ * combinations lap W^a_i - d_i Gamma^a and lap Y_i - d_i Sigma of the gauge
+ * rates are formed before they are rounded to FP32.  For the longitudinal
+ * gauge modes those two terms nearly cancel; rounded separately they leak
+ * FP32 noise into the transverse (magnetic) modes, which sets the FP32
+ * form's B-spectrum error.  Everything else stays FP32.  Needs a tiling
+ * with pair = 1 (and keeps it: other tilings are refused while on); runs
+ * with at most 168 registers whatever reg says.  No counterpart in the
+ * reference. */
+int ewpt_set_fp32_compensated(ewpt_ctx* ctx, int32_t on);
+int32_t ewpt_get_fp32_compensated(const ewpt_ctx* ctx);
 /* Limit of the device-side waits of the TMA-staged stage kernels (pair = 2),
  * in mbarrier polls; polls < 0 restores the default (2^22), 0 makes every
  * wait give up at once.  A wait that runs out ends the kernel's copies

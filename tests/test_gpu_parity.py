@@ -382,6 +382,71 @@ def test_fp32_form_tracks_fp64(ic_kind):
         np.testing.assert_allclose(res[name][3]["mean"][m], s64[m], rtol=1e-4)
 
 
+def test_fp32_compensated_mode_tracks_fp64_closer():
+    """The FP32 form's compensated mode (gauge Laplacians and auxiliary
+    gradients compensated, lap - grad formed before rounding) against FP64 on
+    a thermal 48^3 state (T = 1.5, fields projected onto the Gauss law), 300
+    steps: the B spectrum within 1e-4 per shell and at most half the plain
+    FP32 form's error there, fields closer than the plain form's, energy
+    drift and Gauss violation within 2x of FP64's."""
+    shape = (48, 48, 48)
+    p64 = ewpt.baseline_couplings(shape=shape, N=48, dx=0.25, dt=0.025)
+    p32 = ewpt.baseline_couplings(shape=shape, N=48, dx=0.25, dt=0.025, precision=ewpt.FP32)
+    y0 = ewpt.ic.thermal(shape, 0.25, T=1.5, seed=7, gauss_iters=20)
+    res = {}
+    for name, p, comp in (("64", p64, False), ("32", p32, False), ("32c", p32, True)):
+        with ewpt.Lattice(p) as lat:
+            lat.set_state(y0)
+            if p is p32:
+                lat.set_tiling(8, 16, 2, 1)
+            if comp:
+                lat.set_fp32_compensated(True)
+                assert lat.fp32_compensated()
+            d0 = lat.diagnostics()
+            lat.step(300)
+            res[name] = (lat.get_state(), d0, lat.diagnostics(), lat.spectrum("B", "log", 40)["mean"])
+    y64, d064, d64, s64 = res["64"]
+    m = s64 > 1e-12 * s64.max()
+    drift64 = abs(d64[13] - d064[13])
+    assert drift64 > 1e-3 * abs(d064[13])  # the 2x bar has something to measure
+
+    def errs(name):
+        y, d0, d, sp = res[name]
+        assert np.isfinite(y).all() and np.isfinite(sp).all()
+        field = max(float(np.abs(y[q] - y64[q]).max() / np.abs(y64[q]).max()) for q in range(36))
+        spec = float((np.abs(sp - s64)[m] / s64[m]).max())
+        assert abs(d[13] - d0[13]) <= 2.0 * drift64
+        assert d[14] <= 2.0 * d64[14] and d[16] <= 2.0 * d64[16]
+        return field, spec
+
+    f32, sp32 = errs("32")
+    f32c, sp32c = errs("32c")
+    assert sp32c < 1e-4 and sp32c <= 0.5 * sp32, (sp32c, sp32)
+    assert f32c < f32, (f32c, f32)
+
+
+def test_fp32_compensated_mode_rejections():
+    p64 = ewpt.baseline_couplings(shape=(16, 16, 16), N=16, dx=0.25, dt=0.025)
+    with ewpt.Lattice(p64) as lat, pytest.raises(ewpt.EwptError):
+        lat.set_fp32_compensated(True)  # FP64 context
+    p32 = ewpt.baseline_couplings(shape=(16, 16, 16), N=16, dx=0.25, dt=0.025, precision=ewpt.FP32)
+    with ewpt.Lattice(p32) as lat:
+        with pytest.raises(ewpt.EwptError):
+            lat.set_fp32_compensated(True)  # the default tiling has one site per thread
+        lat.set_tiling(32, 4, 2, 1)
+        lat.set_fp32_compensated(True)
+        for t in ((32, 4, 0, 0), (32, 4, 4, 2)):
+            with pytest.raises(ewpt.EwptError):
+                lat.set_tiling(*t)  # the compensated mode keeps two sites per thread
+        lat.set_tiling(16, 8, 0, 1)
+        lat.set_state(perturbed_bubbles((16, 16, 16), 0.25, 2, seed=3, amp=0.02))  # |Phi| > 0 (the damping's 0/0)
+        lat.step(2)
+        assert np.isfinite(lat.get_state()).all()
+        lat.set_fp32_compensated(False)
+        lat.set_tiling(32, 4, 0, 0)
+        assert not lat.fp32_compensated()
+
+
 @pytest.mark.parametrize("prec", [ewpt.FP64, ewpt.FP32])
 def test_device_bubble_ic_matches_host(prec):
     shape = (24, 20, 18)

@@ -130,6 +130,12 @@ register variant `reg`, `pair` = 1 two sites per thread (FP32 form), 2 TMA tiles
 set_tiling!(L::Lattice, bx, by; reg=0, pair=0) =
     check(ccall((:ewpt_set_tiling, libewpt), Cint, (Ptr{Cvoid}, Int32, Int32, Int32, Int32), L.h, bx, by, reg, pair), L.h)
 
+"""FP32 form, compensated mode (ewpt_set_fp32_compensated): the gauge
+Laplacians and Gauss-auxiliary gradients as float pairs; needs a tiling with
+pair = 1, e.g. `set_tiling!(L, 64, 2; reg=2, pair=1)`."""
+set_fp32_compensated!(L::Lattice, on::Bool=true) =
+    check(ccall((:ewpt_set_fp32_compensated, libewpt), Cint, (Ptr{Cvoid}, Int32), L.h, on ? 1 : 0), L.h)
+
 """Bubble IC on the device (ewpt_init_bubbles; replaces the per-bubble
 `initializer!` launches, main_rk4.jl:4930-4946, :5691-5697).  `bubbles` is
 7 x nb: centre (1-based site indices for profile 0, physical units for
@@ -242,6 +248,10 @@ set_state!(e::Ensemble, m::Integer, y::Array{Float64,4}) =
                     e.h, m, y, 0), e)
 step!(e::Ensemble, nsteps::Integer=1) =
     ens_check(ccall((:ewpt_ensemble_step, libewpt), Cint, (Ptr{Cvoid}, Int32), e.h, nsteps), e)
+"""Launch shape of ensemble member m (0-based; ewpt_ensemble_set_member_tiling)."""
+set_member_tiling!(e::Ensemble, m::Integer, bx, by; reg=2, pair=1) =
+    ens_check(ccall((:ewpt_ensemble_set_member_tiling, libewpt), Cint,
+                    (Ptr{Cvoid}, Int32, Int32, Int32, Int32, Int32), e.h, m, bx, by, reg, pair), e)
 function diagnostics(e::Ensemble, m::Integer)
     out = zeros(Float64, 20)
     ens_check(ccall((:ewpt_ensemble_diagnostics, libewpt), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}), e.h, m, out), e)

@@ -27,3 +27,28 @@ def test_cached_tiling_is_used_without_a_sweep(tmp_path, monkeypatch):
     assert autotune.best_tiling(p) == (64, 2, 2, 1) and len(swept) == 1  # measured, then cached
     assert autotune.best_tiling(p) == (64, 2, 2, 1) and len(swept) == 1  # from the cache
     assert autotune._load_cache()["16x16x16:p1:b0:test-gpu"]["tile"] == [64, 2, 2, 1]
+
+
+def test_member_tilings_sweep_once_per_size(tmp_path, monkeypatch):
+    """The ensemble's per-member shapes: one sweep per distinct member size
+    (no TMA shapes offered; paired shapes only for even nx), cached, and the
+    result mapped back onto every member."""
+    monkeypatch.setenv("EWPT_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_key", lambda p: "x".join(map(str, p.dims)) + ":test-gpu")
+    swept = []
+
+    def fake_sweep(p, steps=2, candidates=None):
+        swept.append((p.dims, list(candidates)))
+        assert not any(t[3] == 2 for t in candidates)
+        best = (8, 16, 2, 1) if p.dims[0] == 48 else (32, 4, 0, 0)
+        return [(t, 1.0 if t == best else 2.0) for t in candidates]
+
+    monkeypatch.setattr(autotune, "sweep", fake_sweep)
+    ps = [ewpt.baseline_couplings(N=n, precision=_lib.FP32) for n in (48, 33, 48, 48, 33)]
+    tiles = autotune.member_tilings(ps)
+    assert tiles == [(8, 16, 2, 1), (32, 4, 0, 0), (8, 16, 2, 1), (8, 16, 2, 1), (32, 4, 0, 0)]
+    assert [d for d, _ in swept] == [(48, 48, 48), (33, 33, 33)]
+    odd = dict(swept)[(33, 33, 33)]
+    assert not any(t[3] for t in odd)  # odd nx: one site per thread only
+    assert (8, 16, 2, 1) in dict(swept)[(48, 48, 48)]
+    assert autotune.member_tilings(ps) == tiles and len(swept) == 2  # from the cache

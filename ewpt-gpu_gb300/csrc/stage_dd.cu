@@ -19,16 +19,78 @@ struct DdBudget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <>
 struct DdBudget<2> { static constexpr int kThreads = 128, kMinBlocks = 3; };
 
+// Stencil sums in double-float with lazy normalisation: each partial sum is
+// an unnormalised pair (h, l), h + l the value, |l| a few ulp of h at most.
+// An addition is Knuth's TwoSum on the high parts plus the low parts (8
+// FP32 operations); a product by a coefficient is the FMA product error
+// plus the cross terms (4).  Only a finished derivative is renormalised
+// (FastTwoSum, 3), where dd's operators renormalise after every operation
+// (11 and 7).  The error per operation stays ~2^-47 of the operands.
+struct Lz {
+    float h, l;
+};
+__device__ __forceinline__ Lz lz_add(const Lz& a, const Lz& b) {
+    const float s = a.h + b.h;
+    const float v = s - a.h;
+    const float e = (a.h - (s - v)) + (b.h - v);
+    return Lz{s, e + (a.l + b.l)};
+}
+__device__ __forceinline__ Lz lz_sub(const Lz& a, const Lz& b) { return lz_add(a, Lz{-b.h, -b.l}); }
+__device__ __forceinline__ Lz lz_mul(const dd& c, const Lz& x) {
+    const float p = c.hi * x.h;
+    float e = fmaf(c.hi, x.h, -p);
+    e = fmaf(c.hi, x.l, e);
+    e = fmaf(c.lo, x.h, e);
+    return Lz{p, e};
+}
+__device__ __forceinline__ dd lz_done(const Lz& x) { return dd_fast_two_sum(x.h, x.l); }
+
 // The stencil evaluations are out-of-line calls: the double-float stage is
 // instruction-fetch bound (~20 k straight-line instructions per site), and
 // one copy of each stencil routine replaces 16 + 4 + 4 inlined copies.
 struct DdAcc : SiteAcc<float2, dd, SrcPtr36<float2>> {
     using Base = SiteAcc<float2, dd, SrcPtr36<float2>>;
-    __device__ __noinline__ void grad_lap(int a, dd& gx, dd& gy, dd& gz, dd& lap) const {
-        Base::grad_lap(a, gx, gy, gz, lap);
+    __device__ __forceinline__ Lz lz(int a, int off) const {
+        const float2 v = __ldg(src.arr(a) + (c + off));
+        return Lz{v.x, v.y};
     }
-    __device__ __noinline__ void grad(int a, dd& gx, dd& gy, dd& gz) const { Base::grad(a, gx, gy, gz); }
-    __device__ __noinline__ dd div3(int a) const { return Base::div3(a); }
+    // derivative along one axis (offsets o) in unnormalised form
+    __device__ __forceinline__ Lz d1_lz(int a, const int* o) const {
+        Lz g = lz_mul(s.a1, lz_sub(lz(a, o[0]), lz(a, o[3])));
+        g = lz_add(g, lz_mul(s.a2, lz_sub(lz(a, o[1]), lz(a, o[4]))));
+        return lz_add(g, lz_mul(s.a3, lz_sub(lz(a, o[2]), lz(a, o[5]))));
+    }
+    __device__ __noinline__ void grad_lap(int a, dd& gx, dd& gy, dd& gz, dd& lap) const {
+        Lz S[3];  // sum over the axes of f(+k) + f(-k), k = 1, 2, 3
+        const int* os[3] = {ox, oy, oz};
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int* o = os[ax];
+            Lz g;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const Lz p = lz(a, o[k]), m = lz(a, o[k + 3]);
+                const dd& ck = k == 0 ? s.a1 : (k == 1 ? s.a2 : s.a3);
+                const Lz t = lz_mul(ck, lz_sub(p, m));
+                g = k == 0 ? t : lz_add(g, t);
+                const Lz q = lz_add(p, m);
+                S[k] = ax == 0 ? q : lz_add(S[k], q);
+            }
+            (ax == 0 ? gx : (ax == 1 ? gy : gz)) = lz_done(g);
+        }
+        Lz L = lz_mul(s.l0, lz(a, 0));
+        L = lz_add(L, lz_mul(s.l1, S[0]));
+        L = lz_add(L, lz_mul(s.l2, S[1]));
+        lap = lz_done(lz_add(L, lz_mul(s.l3, S[2])));
+    }
+    __device__ __noinline__ void grad(int a, dd& gx, dd& gy, dd& gz) const {
+        gx = lz_done(d1_lz(a, ox));
+        gy = lz_done(d1_lz(a, oy));
+        gz = lz_done(d1_lz(a, oz));
+    }
+    __device__ __noinline__ dd div3(int a) const {
+        return lz_done(lz_add(lz_add(d1_lz(a, ox), d1_lz(a + 1, oy)), d1_lz(a + 2, oz)));
+    }
 };
 
 template <int STAGE>

@@ -7,7 +7,8 @@ form) with 8 seeded tanh bubbles and runs one RK4 step in each requested
 form: fp64 (k_stage_fp64), df64 (k_stage_dd, 64x2 tiles, <=168 registers), fp32 (k_stage_fp32,
 64x2 tiles, <=168 registers), fp32x2 (k_stage_fp32x2, two sites per thread, 32x1 tiles),
 fp32x2r2 (k_stage_fp32x2, 64x2 pair-threads, <=168 registers: the tuned 256^3 shape) and fp32tma
-(k_stage_tma, TMA-staged 32x4x4-site tiles; N a multiple of 32).  Meant to
+(k_stage_tma, TMA-staged 32x4x4-site tiles; N a multiple of 32) and fp32c
+(k_stage_fp32x2 in the compensated mode, 64x2 pair-threads).  Meant to
 be wrapped by ncu with -k regex:k_stage.  The form ens runs one step of a
 batched ensemble of FP32-form members of 48^3, 96^3, 96^3 and 128^3 (4.0 M
 sites; the members' k_stage_fp32x2 launches, 16x8 pair-threads), the member mix of the
@@ -21,7 +22,7 @@ from .params import baseline_couplings
 
 TILES = {"fp64": (_lib.FP64, (32, 2, 0, 0)), "df64": (_lib.DF64, (64, 2, 2, 0)), "fp32": (_lib.FP32, (64, 2, 2, 0)),
          "fp32x2": (_lib.FP32, (32, 1, 0, 1)), "fp32x2r2": (_lib.FP32, (64, 2, 2, 1)),
-         "fp32tma": (_lib.FP32, (32, 4, 4, 2))}
+         "fp32tma": (_lib.FP32, (32, 4, 4, 2)), "fp32c": (_lib.FP32, (64, 2, 2, 1))}
 
 
 ENSEMBLE_SIZES = [48, 96, 96, 128]
@@ -55,6 +56,8 @@ def main(argv=None):
             R, w = ic.tanh_profile_params(p.lam, p.vev)
             lat.init_bubbles(ic.tanh_bubble_list(p.dims, p.dx, 8, seed=1), "tanh", R, w)
             lat.set_tiling(*tile)
+            if form == "fp32c":
+                lat.set_fp32_compensated(True)
             lat.step(1)
             lat.sync()
     print("ok")

@@ -13,12 +13,15 @@ lattice and reported in the same line.
 value    FP64 site-updates/s with the state resident in HBM (CUDA events on
          the library's stream; the 4.8 GB state is larger than L2).
 e2e      the same metric through the C ABI with host buffers, as a drop-in
-         rk4_step! caller sees it: every step uploads the state from pinned
-         host memory (ewpt_set_state_packed), steps once (ewpt_step) and
-         reads the evolved state, the step's result, back into pinned host
-         memory (ewpt_get_state_packed).  The snapshot diagnostics are not
-         in the per-step loop: the 256^3 configuration takes them every
-         100 steps, and the reference arm's steps have none either.
+         rk4_step! caller sees it: every step is one ewpt_step_host call
+         that uploads the state from pinned host memory, steps once and
+         writes the evolved state, the step's result, back into pinned host
+         memory, the copies overlapped with stages 1 and 4 over windows of
+         z planes.  `sequential_value` is the same round trip as three calls
+         (ewpt_set_state_packed, ewpt_step, ewpt_get_state_packed).  The
+         snapshot diagnostics are not in the per-step loop: the 256^3
+         configuration takes them every 100 steps, and the reference arm's
+         steps have none either.
 roofline HBM roofline of the stage kernels: algorithmic bytes per
          site-update (3744 B FP64, 2592 B FP32 form) x site-updates/s over
          the measured copy bandwidth.
@@ -218,22 +221,27 @@ def run_ours(args, ws, rank, local):
             import ctypes as C
 
             def e2e_step():
+                ewpt._lib.check(L.ewpt_step_host(lat.h, C.c_void_p(ptr), C.c_void_p(bptr), 1), lat.h)
+
+            def e2e_step_sequential():
                 ewpt._lib.check(L.ewpt_set_state_packed(lat.h, C.c_void_p(ptr), 0), lat.h)
                 ewpt._lib.check(L.ewpt_step(lat.h, 1), lat.h)
                 ewpt._lib.check(L.ewpt_get_state_packed(lat.h, C.c_void_p(bptr), 0), lat.h)
 
-            for _ in range(max(1, min(args.warmup, 2))):
-                e2e_step()
             ke = max(1, args.steps)
-            barrier(ws)
-            t0 = time.perf_counter()
-            for _ in range(ke):
-                e2e_step()
-            te = allmax(ws, time.perf_counter() - t0)
-            # the step's result arrived in host memory: check it is a finite state
-            assert np.isfinite(back.numpy()[:, :: max(1, S // 4096)]).all()
+            te = {}
+            for name, fn in (("sequential", e2e_step_sequential), ("overlapped", e2e_step)):
+                for _ in range(max(1, min(args.warmup, 2))):
+                    fn()
+                barrier(ws)
+                t0 = time.perf_counter()
+                for _ in range(ke):
+                    fn()
+                te[name] = allmax(ws, time.perf_counter() - t0)
+                # the step's result arrived in host memory: check it is a finite state
+                assert np.isfinite(back.numpy()[:, :: max(1, S // 4096)]).all()
             ewpt._lib.check(L.ewpt_diagnostics(lat.h, row.ctypes.data_as(ewpt._lib.DP)), lat.h)  # after the timing
-            res["e2e"] = dict(t=te, steps=ke, h2d=36 * S * 8, d2h=36 * S * 8)
+            res["e2e"] = dict(t=te["overlapped"], t_seq=te["sequential"], steps=ke, h2d=36 * S * 8, d2h=36 * S * 8)
     # ---------------------------------------------------------------- FP32
     if not args.no_fp32:
         p32 = make_params(n, ewpt.FP32)
@@ -325,8 +333,12 @@ def run_ours(args, ws, rank, local):
         e = res["e2e"]
         out["e2e"] = {"value": ws * S * e["steps"] / e["t"], "unit": "site-updates/s",
                       "h2d_bytes_per_step": e["h2d"], "d2h_bytes_per_step": e["d2h"], "steps": e["steps"],
-                      "path": "ewpt_set_state_packed(pinned host) + ewpt_step(1) + "
-                              "ewpt_get_state_packed(pinned host) per step"}
+                      "ms_per_step": e["t"] / e["steps"] * 1e3,
+                      "path": "ewpt_step_host(pinned host in, pinned host out, 1 step) per step: upload "
+                              "overlapped with stage 1, download with stage 4 (windows of z planes)",
+                      "sequential_value": ws * S * e["steps"] / e["t_seq"],
+                      "sequential_path": "ewpt_set_state_packed(pinned host) + ewpt_step(1) + "
+                                         "ewpt_get_state_packed(pinned host) per step"}
     if "fp32" in res:
         f = res["fp32"]
         v32 = ws * S * f["steps"] / f["t"]

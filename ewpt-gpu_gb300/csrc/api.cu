@@ -221,10 +221,10 @@ constexpr size_t kChunkMin = (size_t)64 << 20;
 
 static cudaError_t io_streams(ewpt_ctx* c) {
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < kChunks - 1 && e == cudaSuccess; ++i)
-        if (!c->io_st[i]) e = cudaStreamCreateWithFlags(&c->io_st[i], cudaStreamNonBlocking);
-    for (int i = 0; i < kChunks && e == cudaSuccess; ++i)
-        if (!c->io_ev[i]) e = cudaEventCreateWithFlags(&c->io_ev[i], cudaEventDisableTiming);
+    for (cudaStream_t& s : c->io_st)
+        if (!s && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    for (cudaEvent_t& ev : c->io_ev)
+        if (!ev && e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     return e;
 }
 
@@ -376,6 +376,124 @@ static int do_steps(ewpt_ctx* c, int32_t nsteps, bool expl, double Jex, double g
 }
 
 int ewpt_step(ewpt_ctx* c, int32_t nsteps) { return do_steps(c, nsteps, false, 0.0, 0.0); }
+
+// ---- host-to-host steps
+// True when [p, p + bytes) is page-locked host memory (cudaHostAlloc or
+// cudaHostRegister), which asynchronous copies can overlap with kernels.
+static bool pinned_host(const void* p, size_t bytes) {
+    const char* q[2] = {static_cast<const char*>(p), static_cast<const char*>(p) + bytes - 1};
+    for (const char* x : q) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, x) != cudaSuccess) {
+            cudaGetLastError();  // not a sticky error: clear it
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
+// Upload (FP64 form, 6th-order stencils, pinned buffers): the state goes up
+// in nwin windows of z planes, each window's 36 array pieces spread over
+// the four io streams.  Stage 1 of the first step runs on the planes whose
+// 3-plane neighbourhood has arrived while the next windows are in flight;
+// stage 4 of the last step runs window by window, and each finished window
+// goes down while the next is computed.  Every site sees the arithmetic of
+// a whole-lattice launch, so the result is the one of set_state_packed +
+// step + get_state_packed, bit for bit.
+static int step_host_overlapped(ewpt_ctx* c, const double* in, double* out, int32_t nsteps) {
+    const Grid& g = c->g;
+    const int nz = g.nz, nio = 4;
+    const int nwin = std::max(2, std::min(8, nz / 16));
+    const int64_t S = g.S, A = (int64_t)g.nx * g.ny;
+    int zw[9];
+    for (int w = 0; w <= nwin; ++w) zw[w] = (int)((int64_t)nz * w / nwin);
+    cudaError_t e = io_streams(c);
+    // the io streams start after the work queued on the context's stream
+    auto fork = [&]() {
+        if (e == cudaSuccess) e = cudaEventRecord(c->io_ev[4], c->st);
+        for (int i = 0; i < nio && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(c->io_st[i], c->io_ev[4], 0);
+    };
+    // the context's stream waits for every copy queued so far
+    auto join = [&]() {
+        for (int i = 0; i < nio && e == cudaSuccess; ++i) {
+            e = cudaEventRecord(c->io_ev[i], c->io_st[i]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->st, c->io_ev[i], 0);
+        }
+    };
+    auto copy_window = [&](int w, bool up) {
+        const int64_t off = zw[w] * A;
+        const size_t bytes = (size_t)(zw[w + 1] - zw[w]) * A * sizeof(double);
+        for (int a = 0; a < 36 && e == cudaSuccess; ++a) {
+            double* dev = c->y + a * S + off;
+            const int64_t h = a * S + off;
+            e = up ? cudaMemcpyAsync(dev, in + h, bytes, cudaMemcpyHostToDevice, c->io_st[a % nio])
+                   : cudaMemcpyAsync(out + h, dev, bytes, cudaMemcpyDeviceToHost, c->io_st[a % nio]);
+        }
+    };
+    auto stage = [&](int s, int k0, int k1, double J, double G) {
+        if (e == cudaSuccess)
+            e = launch_stage_fp64_planes(g, c->tile, s, k0, k1, c->y, c->yn, c->xa, c->xb, c->p, J, G, c->st);
+    };
+    for (int32_t s = 0; s < nsteps && e == cudaSuccess; ++s) {
+        const int64_t it = c->it + 1 + s;
+        const double J = jext_of(c->p, it), G = damp_of(c->p, it);
+        if (s == 0) {
+            fork();
+            int lo = 3;  // planes [3, lo) have had stage 1
+            for (int w = 0; w < nwin; ++w) {
+                copy_window(w, true);
+                join();
+                const int hi = w == nwin - 1 ? nz : zw[w + 1] - 3;
+                if (hi > lo) {
+                    stage(1, lo, hi, J, G);
+                    lo = hi;
+                }
+            }
+            stage(1, 0, 3, J, G);  // their lower neighbours wrap to the top planes
+        } else {
+            stage(1, 0, nz, J, G);
+        }
+        stage(2, 0, nz, J, G);
+        stage(3, 0, nz, J, G);
+        if (s < nsteps - 1) {
+            stage(4, 0, nz, J, G);
+            continue;
+        }
+        for (int w = 0; w < nwin; ++w) {
+            stage(4, zw[w], zw[w + 1], J, G);
+            fork();
+            copy_window(w, false);
+        }
+        join();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {  // drain what was queued before reporting
+        for (cudaStream_t st : c->io_st)
+            if (st) cudaStreamSynchronize(st);
+        cudaStreamSynchronize(c->st);
+        return ewpt_cuda_check(c, e, "step_host");
+    }
+    c->it += nsteps;
+    return EWPT_OK;
+}
+
+int ewpt_step_host(ewpt_ctx* c, const double* state_in, double* state_out, int32_t nsteps) {
+    if (!c) return ewpt_fail(nullptr, EWPT_ERR_ARG, "ctx is NULL");
+    if (!state_in || !state_out) return ewpt_fail(c, EWPT_ERR_ARG, "state_in or state_out is NULL");
+    if (nsteps < 0) return ewpt_fail(c, EWPT_ERR_ARG, "nsteps < 0");
+    if (c->view) return ewpt_fail(c, EWPT_ERR_STATE, "this context is a read-only view");
+    if (c->slab) return ewpt_fail(c, EWPT_ERR_STATE, "a slab steps stage by stage between ghost exchanges");
+    cudaSetDevice(c->p.device);
+    const size_t bytes = (size_t)36 * c->g.S * sizeof(double);
+    if (nsteps > 0 && c->p.precision == EWPT_FP64 && c->p.stencil_order == 6 && c->g.nz >= 16 &&
+        pinned_host(state_in, bytes) && pinned_host(state_out, bytes))
+        return step_host_overlapped(c, state_in, state_out, nsteps);
+    int rc = ewpt_set_state_packed(c, state_in, 0);
+    if (!rc) rc = ewpt_step(c, nsteps);
+    if (!rc) rc = ewpt_get_state_packed(c, state_out, 0);
+    return rc;
+}
 
 int ewpt_step_explicit(ewpt_ctx* c, int32_t nsteps, double Jex, double gamma) {
     return do_steps(c, nsteps, true, Jex, gamma);

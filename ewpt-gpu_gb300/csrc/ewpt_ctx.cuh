@@ -31,9 +31,11 @@ struct ewpt_ctx {
     int64_t wait_polls = -1;  // limit of the TMA kernels' mbarrier waits in polls (< 0: default)
     Fp32Work w32{nullptr, nullptr, nullptr};
     bool fp32_comp = false;  // FP32 form: compensated gauge stencils (ewpt_set_fp32_compensated)
-    // side streams and events of the chunked host <-> device state copies (api.cu copy_runs)
-    cudaStream_t io_st[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // side streams and events of the host <-> device state copies: the
+    // chunked copies (api.cu copy_runs) use io_st[0..2] and io_ev[0..3], the
+    // overlapped host-to-host steps (ewpt_step_host) all of them
+    cudaStream_t io_st[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t io_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // [36][S] doubles: FP64 view of an FP32 state (diagnostics, get/set)
     double* scratch64 = nullptr;
     // diagnostics / spectra scratch (diag.cu, spectrum.cu)

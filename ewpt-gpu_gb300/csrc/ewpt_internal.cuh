@@ -17,6 +17,9 @@ struct Grid {
     int nx, ny, nz;
     int64_t S;  // nx*ny*nz, or the padded array stride of a slab
     int zg = 0;
+    // FP64 stage launches over a window of z planes: the launch's block z
+    // index b covers plane k0 + b (0 for whole-lattice launches)
+    int k0 = 0;
 };
 
 // Storage of one FP32-form [36][.] array set: element (i, j, k) of array a
@@ -166,6 +169,14 @@ cudaError_t launch_step_fp64(const Grid& g, const Tiling& t, double* y, double* 
 // One stage (1..4) of that step (z-slabs exchange ghost planes between stages).
 cudaError_t launch_stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa,
                               double* xb, const ewpt_params& p, double Jex, double gam, cudaStream_t st);
+// The same stage over the z planes [k0, k1) only: those sites' outputs are
+// what a whole-lattice launch writes for them, bit for bit, and no other
+// site is written.  Reads the stage input on planes [k0 - 3, k1 + 3)
+// (periodic).  Lets a host-to-host step start stage 1 on the planes already
+// uploaded and download the planes stage 4 has finished.
+cudaError_t launch_stage_fp64_planes(const Grid& g, const Tiling& t, int stage, int k0, int k1, double* y,
+                                     double* yn, double* xa, double* xb, const ewpt_params& p, double Jex,
+                                     double gam, cudaStream_t st);
 // FP64 stage and rates with the alternative stencil orders (stage_orders.cu)
 cudaError_t launch_step_fp64_order(const Grid& g, const Tiling& t, double* y, double* yn, double* xa, double* xb,
                                    const ewpt_params& p, double Jex, double gam, cudaStream_t st);

@@ -44,7 +44,7 @@ template <typename TL, typename T>
 __device__ __forceinline__ bool make_acc(const Grid& g, const StencilCoef<T>& sc, GlobalAcc<TL, T>& A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+    const int k = blockIdx.z + g.k0;
     if (i >= g.nx || j >= g.ny) return false;
     A.place(i, j, k, g.nx, g.ny, g.nz, g.zg);
     A.s = sc;
@@ -271,10 +271,14 @@ static void step_fp64(const Grid& g, const Tiling& t, double* y, double* yn, dou
     k_stage_fp64<4, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, nullptr, y, pc, sc, dt / 6., 0.0);
 }
 
+// planes g.k0 .. g.k0 + nzl - 1
 template <bool BETA, int REG>
 static void stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa, double* xb,
-                       const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
-    const dim3 gr = grid_of(g, t), bl(t.bx, t.by);
+                       const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st,
+                       int nzl) {
+    dim3 gr = grid_of(g, t);
+    gr.z = nzl;
+    const dim3 bl(t.bx, t.by);
     switch (stage) {
         case 1: k_stage_fp64<1, BETA, REG><<<gr, bl, 0, st>>>(g, pack(y, g.S, 8), y, yn, xa, nullptr, pc, sc, dt / 6., dt / 2.); break;
         case 2: k_stage_fp64<2, BETA, REG><<<gr, bl, 0, st>>>(g, pack(xa, g.S, 8), y, yn, xb, nullptr, pc, sc, dt / 3., dt / 2.); break;
@@ -285,23 +289,35 @@ static void stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, dou
 
 template <bool BETA>
 static void stage_fp64_r(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa, double* xb,
-                         const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st) {
+                         const PhysCoef<double>& pc, const StencilCoef<double>& sc, double dt, cudaStream_t st,
+                         int nzl) {
     if (t.reg == 1)
-        stage_fp64<BETA, 1>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+        stage_fp64<BETA, 1>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st, nzl);
     else if (t.reg == 2)
-        stage_fp64<BETA, 2>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+        stage_fp64<BETA, 2>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st, nzl);
     else
-        stage_fp64<BETA, 0>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st);
+        stage_fp64<BETA, 0>(g, t, stage, y, yn, xa, xb, pc, sc, dt, st, nzl);
 }
 
 cudaError_t launch_stage_fp64(const Grid& g, const Tiling& t, int stage, double* y, double* yn, double* xa,
                               double* xb, const ewpt_params& p, double Jex, double gam, cudaStream_t st) {
+    Grid gw = g;
+    gw.k0 = 0;
+    return launch_stage_fp64_planes(gw, t, stage, 0, g.nz, y, yn, xa, xb, p, Jex, gam, st);
+}
+
+cudaError_t launch_stage_fp64_planes(const Grid& g, const Tiling& t, int stage, int k0, int k1, double* y,
+                                     double* yn, double* xa, double* xb, const ewpt_params& p, double Jex,
+                                     double gam, cudaStream_t st) {
+    if (k0 < 0 || k1 > g.nz || k0 >= k1) return k0 == k1 ? cudaSuccess : cudaErrorInvalidValue;
     const PhysCoef<double> pc = make_phys<double>(p, Jex, gam);
     const StencilCoef<double> sc = make_stencil<double>(p.dx);
+    Grid gw = g;
+    gw.k0 = k0;
     if (p.beta_w != 0.0 || p.beta_y != 0.0)
-        stage_fp64_r<true>(g, t, stage, y, yn, xa, xb, pc, sc, p.dt, st);
+        stage_fp64_r<true>(gw, t, stage, y, yn, xa, xb, pc, sc, p.dt, st, k1 - k0);
     else
-        stage_fp64_r<false>(g, t, stage, y, yn, xa, xb, pc, sc, p.dt, st);
+        stage_fp64_r<false>(gw, t, stage, y, yn, xa, xb, pc, sc, p.dt, st, k1 - k0);
     return cudaGetLastError();
 }
 

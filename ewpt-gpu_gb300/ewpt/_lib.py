@@ -60,6 +60,7 @@ def _sig(L):
     L.ewpt_get_state_packed.argtypes = [V, C.c_void_p, C.c_int32]
     L.ewpt_step.argtypes = [V, C.c_int32]
     L.ewpt_step_explicit.argtypes = [V, C.c_int32, C.c_double, C.c_double]
+    L.ewpt_step_host.argtypes = [V, C.c_void_p, C.c_void_p, C.c_int32]
     L.ewpt_iteration.argtypes = [V]
     L.ewpt_iteration.restype = C.c_int64
     L.ewpt_sync.argtypes = [V]

@@ -84,6 +84,31 @@ class Lattice:
         else:
             self._chk(self.L.ewpt_step_explicit(self.h, int(n), float(Jex or 0.0), float(gamma or 0.0)))
 
+    def step_host(self, state_in, state_out, n: int = 1):
+        """Host state in, n RK4 steps, host state out (ewpt_step_host).
+
+        state_in / state_out: C-contiguous float64 buffers of shape (36, S),
+        numpy arrays or CPU torch tensors (may be the same object).  With
+        page-locked buffers (``torch.empty(..., pin_memory=True)``) the copies
+        of an FP64 lattice overlap the first and last steps' stencil work;
+        the result is that of set_state + step(n) + get_state in any case.
+        """
+        ptrs = []
+        for buf in (state_in, state_out):
+            if hasattr(buf, "data_ptr"):
+                ok = buf.dtype == __import__("torch").float64 and buf.is_contiguous() and not buf.is_cuda
+                ptr, shape = buf.data_ptr(), tuple(buf.shape)
+            else:
+                ok = isinstance(buf, np.ndarray) and buf.dtype == np.float64 and buf.flags.c_contiguous
+                ptr, shape = (buf.ctypes.data if ok else 0), buf.shape
+            if not ok or shape != (36, self.S):
+                raise ValueError(f"host states must be C-contiguous float64 of shape (36, {self.S})")
+            ptrs.append(ptr)
+        if not ptrs[1] or getattr(state_out, "flags", None) is not None and not state_out.flags.writeable:
+            raise ValueError("state_out must be writeable")
+        self._chk(self.L.ewpt_step_host(self.h, C.c_void_p(ptrs[0]), C.c_void_p(ptrs[1]), int(n)))
+        return state_out
+
     def sync(self):
         self._chk(self.L.ewpt_sync(self.h))
 

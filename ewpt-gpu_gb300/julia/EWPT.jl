@@ -76,6 +76,18 @@ end
 """nsteps RK4 steps with the J_ext/damp schedule of main_rk4.jl:5154-5172."""
 step!(L::Lattice, nsteps::Integer=1) = check(ccall((:ewpt_step, libewpt), Cint, (Ptr{Cvoid}, Int32), L.h, nsteps), L.h)
 
+"""Host state in, nsteps RK4 steps, host state out (ewpt_step_host): `y_in` and
+`y_out` are nx x ny x nz x 36 Float64 arrays (may be the same array).  With
+page-locked arrays (`Base.Libc` memory registered by `CUDA.Mem.register`, or
+any cudaHostRegister'ed buffer) the copies overlap the stencil work."""
+function step_host!(y_out::Array{Float64,4}, L::Lattice, y_in::Array{Float64,4}, nsteps::Integer=1)
+    n = 36 * Int(L.p.nx) * Int(L.p.ny) * Int(L.p.nz)
+    length(y_in) == n && length(y_out) == n || error("y_in and y_out must hold 36 nx ny nz values")
+    GC.@preserve y_in y_out check(ccall((:ewpt_step_host, libewpt), Cint,
+                                        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int32), L.h, y_in, y_out, nsteps), L.h)
+    y_out
+end
+
 """The 20-column snapshot row (13 reference columns + total + Gauss columns)."""
 function diagnostics(L::Lattice)
     out = zeros(Float64, 20)

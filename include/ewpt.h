@@ -105,6 +105,20 @@ int ewpt_get_state_packed(ewpt_ctx* ctx, double* buf, int32_t on_device);
 int ewpt_step(ewpt_ctx* ctx, int32_t nsteps);
 /* Same with explicit Jex and gamma for every step (counter still advances). */
 int ewpt_step_explicit(ewpt_ctx* ctx, int32_t nsteps, double Jex, double gamma);
+/* Host state in, nsteps RK4 steps, host state out, synchronous: the same
+ * result as ewpt_set_state_packed(state_in, 0) + ewpt_step(nsteps) +
+ * ewpt_get_state_packed(state_out, 0), bit for bit, and the same iteration
+ * count and drive.  Both buffers hold 36*nx*ny*nz doubles (array-major) and
+ * may be the same buffer; the new state also stays on the device.  FP64
+ * contexts with 6th-order stencils, nz >= 16 and page-locked buffers
+ * (cudaHostAlloc / cudaHostRegister) overlap the copies with the stencil
+ * work: the upload goes in windows of z planes, stage 1 of the first step
+ * starts on the planes that have arrived, and the planes that stage 4 of the
+ * last step has finished go down while the rest is computed.  Other
+ * contexts and pageable buffers take the three calls in turn.  Replaces the
+ * copyto!(CuArray, Array) ... rk4 loop ... Array(CuArray) round trip of a
+ * host-side driver (main_rk4.jl:5174-5304, 6146-6437). */
+int ewpt_step_host(ewpt_ctx* ctx, const double* state_in, double* state_out, int32_t nsteps);
 /* Iterations done so far (the `it` of the reference loop). */
 int64_t ewpt_iteration(const ewpt_ctx* ctx);
 /* Launch shape of the stage kernels.  pair = 0 or 1: blocks of bx*by

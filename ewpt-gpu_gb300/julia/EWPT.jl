@@ -78,8 +78,9 @@ step!(L::Lattice, nsteps::Integer=1) = check(ccall((:ewpt_step, libewpt), Cint, 
 
 """Host state in, nsteps RK4 steps, host state out (ewpt_step_host): `y_in` and
 `y_out` are nx x ny x nz x 36 Float64 arrays (may be the same array).  With
-page-locked arrays (`Base.Libc` memory registered by `CUDA.Mem.register`, or
-any cudaHostRegister'ed buffer) the copies overlap the stencil work."""
+page-locked arrays (registered with cudaHostRegister, e.g. through
+`CUDA.Mem.register`) an FP64 lattice overlaps the copies with the stencil
+work; the result is that of set_state! + step! + get_state! in any case."""
 function step_host!(y_out::Array{Float64,4}, L::Lattice, y_in::Array{Float64,4}, nsteps::Integer=1)
     n = 36 * Int(L.p.nx) * Int(L.p.ny) * Int(L.p.nz)
     length(y_in) == n && length(y_out) == n || error("y_in and y_out must hold 36 nx ny nz values")

@@ -43,6 +43,7 @@ static int host_checks(void) {
     CHECK(ewpt_create(&p, &ctx) == EWPT_ERR_ARG && ctx == NULL, "create rejects nx < 7");
     CHECK(strlen(ewpt_last_error(NULL)) > 0, "error message");
     CHECK(ewpt_step(NULL, 1) == EWPT_ERR_ARG, "step rejects NULL ctx");
+    CHECK(ewpt_step_host(NULL, NULL, NULL, 1) == EWPT_ERR_ARG, "step_host rejects NULL ctx");
     CHECK(ewpt_field_components(EWPT_FIELD_DENSITY) == 7 && ewpt_field_components(99) == -1, "field components");
     CHECK(ewpt_kc_bin_nums(4, 4, 4) > 0 && ewpt_kc_bin_nums(0, 4, 4) == -1, "kc_bin_nums");
     printf("host ok\n");

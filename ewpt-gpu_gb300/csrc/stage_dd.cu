@@ -161,7 +161,7 @@ __global__ void k_from_dd(int64_t n, const double* __restrict__ src, double* __r
 }
 
 
-// One stage: the whole stage with beta terms, else its two halves.
+// One stage: the whole stage with beta terms, else its three parts.
 template <int STAGE, bool BETA, int REG>
 void stage_dd(const dim3& gr, const dim3& bl, cudaStream_t st, const Grid& g, const float2* X, const float2* y,
               float2* yn, float2* xn, float2* acc_out, const PhysCoef<dd>& pc, const StencilCoef<dd>& sc, dd w,

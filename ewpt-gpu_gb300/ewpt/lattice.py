@@ -93,21 +93,26 @@ class Lattice:
         of an FP64 lattice overlap the first and last steps' stencil work;
         the result is that of set_state + step(n) + get_state in any case.
         """
-        ptrs = []
-        for buf in (state_in, state_out):
-            if hasattr(buf, "data_ptr"):
-                ok = buf.dtype == __import__("torch").float64 and buf.is_contiguous() and not buf.is_cuda
-                ptr, shape = buf.data_ptr(), tuple(buf.shape)
-            else:
-                ok = isinstance(buf, np.ndarray) and buf.dtype == np.float64 and buf.flags.c_contiguous
-                ptr, shape = (buf.ctypes.data if ok else 0), buf.shape
-            if not ok or shape != (36, self.S):
-                raise ValueError(f"host states must be C-contiguous float64 of shape (36, {self.S})")
-            ptrs.append(ptr)
-        if not ptrs[1] or getattr(state_out, "flags", None) is not None and not state_out.flags.writeable:
+        ptrs = [self._host_state_ptr(state_in, "state_in"), self._host_state_ptr(state_out, "state_out")]
+        if isinstance(state_out, np.ndarray) and not state_out.flags.writeable:
             raise ValueError("state_out must be writeable")
         self._chk(self.L.ewpt_step_host(self.h, C.c_void_p(ptrs[0]), C.c_void_p(ptrs[1]), int(n)))
         return state_out
+
+    def _host_state_ptr(self, buf, name: str) -> int:
+        """Address of a (36, S) C-contiguous float64 host buffer: a numpy
+        array or a CPU torch tensor."""
+        if isinstance(buf, np.ndarray):
+            ok = buf.dtype == np.float64 and buf.flags.c_contiguous
+            ptr = buf.ctypes.data
+        elif hasattr(buf, "data_ptr") and hasattr(buf, "is_cuda"):
+            ok = str(buf.dtype) == "torch.float64" and buf.is_contiguous() and not buf.is_cuda
+            ptr = buf.data_ptr()
+        else:
+            ok, ptr = False, 0
+        if not ok or tuple(buf.shape) != (36, self.S):
+            raise ValueError(f"{name} must be a C-contiguous float64 host buffer of shape (36, {self.S})")
+        return ptr
 
     def sync(self):
         self._chk(self.L.ewpt_sync(self.h))

@@ -91,3 +91,27 @@ def test_surrogate_parameter_draws():
     np.testing.assert_array_equal(prm, prm2)
     _, prm1, _ = surrogate.draw_members(10, 24, seed=1)
     assert prm1.shape == (10, 4)
+
+
+def test_step_host_buffer_checks():
+    """Lattice.step_host takes (36, S) C-contiguous float64 host buffers,
+    numpy or CPU torch, and refuses anything else before any library call."""
+    import pytest
+    import torch
+
+    from ewpt.lattice import Lattice
+
+    lat = Lattice.__new__(Lattice)  # no device context: only the checks run
+    lat.S = 12
+    good = [np.zeros((36, 12)), torch.zeros((36, 12), dtype=torch.float64)]
+    for buf in good:
+        assert Lattice._host_state_ptr(lat, buf, "state_in") != 0
+    bad = [np.zeros((36, 12), np.float32), np.zeros((36, 11)), np.zeros((12, 36)).T,
+           torch.zeros((36, 12)), torch.zeros((36, 24), dtype=torch.float64)[:, ::2], [0.0] * 432]
+    for buf in bad:
+        with pytest.raises(ValueError, match="state_in"):
+            Lattice._host_state_ptr(lat, buf, "state_in")
+    ro = np.zeros((36, 12))
+    ro.flags.writeable = False
+    with pytest.raises(ValueError, match="writeable"):
+        lat.step_host(np.zeros((36, 12)), ro, 1)

@@ -401,12 +401,14 @@ static bool pinned_host(const void* p, size_t bytes) {
 // goes down while the next is computed.  Every site sees the arithmetic of
 // a whole-lattice launch, so the result is the one of set_state_packed +
 // step + get_state_packed, bit for bit.
+constexpr int kHostWindows = 8;  // at most; at least 16 planes per window
+
 static int step_host_overlapped(ewpt_ctx* c, const double* in, double* out, int32_t nsteps) {
     const Grid& g = c->g;
     const int nz = g.nz, nio = 4;
-    const int nwin = std::max(2, std::min(8, nz / 16));
+    const int nwin = std::max(2, std::min(kHostWindows, nz / 16));
     const int64_t S = g.S, A = (int64_t)g.nx * g.ny;
-    int zw[9];
+    int zw[kHostWindows + 1];
     for (int w = 0; w <= nwin; ++w) zw[w] = (int)((int64_t)nz * w / nwin);
     cudaError_t e = io_streams(c);
     // the io streams start after the work queued on the context's stream

@@ -401,7 +401,7 @@ static bool pinned_host(const void* p, size_t bytes) {
 // goes down while the next is computed.  Every site sees the arithmetic of
 // a whole-lattice launch, so the result is the one of set_state_packed +
 // step + get_state_packed, bit for bit.
-constexpr int kHostWindows = 8;  // at most; at least 16 planes per window
+constexpr int kHostWindows = 8;  // windows per host step: min(8, nz / 16), at least 2
 
 static int step_host_overlapped(ewpt_ctx* c, const double* in, double* out, int32_t nsteps) {
     const Grid& g = c->g;

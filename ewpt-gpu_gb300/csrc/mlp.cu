@@ -10,7 +10,7 @@
 // gradients enter the GEMMs as BF16, pre-activations and accumulations stay
 // FP32.  This network has no counterpart in the reference: it maps early-time
 // spectra of the evolution to late-time magnetic spectra for parameter
-// sweeps, and the evolution itself stays the fallback and the judge.
+// sweeps, and the evolution itself stays the fallback and the reference answer.
 #include <cuda_bf16.h>
 
 #include <algorithm>

@@ -6,8 +6,8 @@ and backward kernels and AdamW) maps the early-time spectra of a run (B and
 Higgs, `nshell` log shells each) plus its parameters (lambda, g, g', bubble
 count) to the late-time log B spectrum.  Training data come from the
 library's batched ensemble engine (seeded uniform parameter draws, device
-bubble or thermal ICs); the plain evolution is the fallback and the judge of the
-surrogate's error, and the surrogate never replaces the evolution path.
+bubble or thermal ICs); the plain evolution is the fallback and the yardstick of
+the surrogate's error, and the surrogate never replaces the evolution path.
 """
 from __future__ import annotations
 
@@ -226,7 +226,7 @@ def train_and_evaluate(n_runs: int = 1024, N=48, nshell: int = 40, t_early: int 
                        thermal_fraction: float = 0.0) -> dict:
     """Generate a dataset with the ensemble engine, train the surrogate on the
     growth of the log B spectrum over persistence, and report held-out errors
-    against the evolved spectra (the judge) and the cost of both paths.
+    against the evolved spectra (the reference answer) and the cost of both paths.
     holdout: a fraction of the runs (< 1) or a number of runs (>= 1)."""
     t_gen = time.perf_counter()
     data = generate_dataset(n_runs, N=N, nshell=nshell, t_early=t_early, t_late=t_late, seed=seed,

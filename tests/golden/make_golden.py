@@ -23,7 +23,7 @@ precision on seeded inputs:
 
 The RK4 combination of the driver loop (main_rk4.jl:6182-6435) lives inside
 `run()` and is restated here as its four broadcast lines (mul, then add).
-The fixtures are committed; the GPU machine never reads the reference.
+The fixtures are committed; the tests never read the reference at run time.
 """
 from __future__ import annotations
 

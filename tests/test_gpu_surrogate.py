@@ -2,7 +2,7 @@
 seeds it predicts the late-time log B spectrum far better than the
 input-blind baseline (the training-set mean spectrum) and than persistence
 (the early spectrum shifted by the mean growth), at a small fraction of the
-cost of evolving the run.  The evolution remains the judge: the errors are
+cost of evolving the run.  The evolution remains the reference answer: the errors are
 measured against evolved spectra."""
 import time
 
